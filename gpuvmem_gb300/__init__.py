@@ -1,0 +1,272 @@
+"""gpuvmem_gb300: GB300-native imaging-objective path of gpuvmem.
+
+Python view of the C ABI in include/gpuvmem_gb300.h (ctypes).  Device
+buffers are torch CUDA tensors; torch is used for device memory and streams
+only -- every computation runs in the in-tree CUDA library
+libgpuvmem_gb300.so.  There is no CPU fallback: if the library is missing
+the import of `lib()` raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgpuvmem_gb300.so")
+_LIB = None
+
+GV_OK = 0
+STATUS = {0: "GV_OK", 1: "GV_ERR_INVALID", 2: "GV_ERR_CUDA", 3: "GV_ERR_NOMEM",
+          4: "GV_ERR_UNSUPPORTED", 5: "GV_ERR_DEVICE"}
+FI_CHI2, FI_ENTROPY, FI_TSV, FI_TV, FI_L1, FI_LAPLACIAN = range(6)
+FI_IDS = {"Chi2": FI_CHI2, "Entropy": FI_ENTROPY, "TotalSquaredVariation": FI_TSV,
+          "TotalVariation": FI_TV, "L1-Norm": FI_L1, "Laplacian": FI_LAPLACIAN}
+OPT_FRPRMN, OPT_LBFGS = 0, 1
+OPT_IDS = {"CG-FRPRMN": OPT_FRPRMN, "CG-LBFGS": OPT_LBFGS}
+
+
+class GvError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class FiDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("lam", C.c_float), ("image_index", C.c_int32),
+                ("image_to_add", C.c_int32), ("prior_value", C.c_float), ("eta", C.c_float),
+                ("epsilon", C.c_float)]
+
+
+class ChannelDesc(C.Structure):
+    _fields_ = [("freq_hz", C.c_float), ("nvis", C.c_int64), ("uvw", C.POINTER(C.c_double)),
+                ("vo", C.POINTER(C.c_float)), ("weight", C.POINTER(C.c_float))]
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("M", C.c_int32), ("N", C.c_int32), ("deltax_deg", C.c_double),
+                ("deltay_deg", C.c_double), ("xobs_pix", C.c_float), ("yobs_pix", C.c_float),
+                ("nu_0", C.c_float), ("antenna_diameter", C.c_float), ("pb_factor", C.c_float),
+                ("pb_cutoff", C.c_float), ("primary_beam", C.c_int32), ("vis_noise", C.c_float),
+                ("noise_cut_factor", C.c_float), ("eta", C.c_float),
+                ("initial_value", C.c_float), ("threshold", C.c_float),
+                ("normalize", C.c_int32), ("nchannels", C.c_int32),
+                ("channels", C.POINTER(ChannelDesc)), ("nterms", C.c_int32),
+                ("terms", C.POINTER(FiDesc)), ("dchi2_engine", C.c_int32)]
+
+
+class ProblemInfo(C.Structure):
+    _fields_ = [("fg_scale", C.c_float), ("noise_cut", C.c_float), ("vis_noise", C.c_float),
+                ("minpix", C.c_float), ("beam_bmaj_deg", C.c_double),
+                ("beam_bmin_deg", C.c_double), ("beam_bpa_deg", C.c_double),
+                ("sum_weights", C.c_float), ("nvis_total", C.c_int64),
+                ("nvis_in_grid", C.c_int64), ("mask_pixels", C.c_int64),
+                ("dchi2_engine", C.c_int32), ("nterms", C.c_int32)]
+
+
+class OptDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("total_iterations", C.c_int32), ("ftol", C.c_float),
+                ("gtol", C.c_float), ("K", C.c_int32), ("flag", C.c_int32),
+                ("positivity", C.c_int32)]
+
+
+class OptReport(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("exit_reason", C.c_int32), ("f_final", C.c_float),
+                ("n_objective", C.c_int64), ("n_gradient", C.c_int64), ("seconds", C.c_double)]
+
+
+EXPORTS = ["gv_problem_create", "gv_problem_destroy", "gv_problem_info_get",
+           "gv_problem_set_stream", "gv_noise_image", "gv_initial_image", "gv_chi2", "gv_dchi2",
+           "gv_dchi2_channel", "gv_prior_value", "gv_prior_gradient", "gv_objective",
+           "gv_gradient", "gv_optimize", "gv_dirty_image", "gv_residuals", "gv_last_error",
+           "gv_version"]
+
+
+def lib():
+    """Load libgpuvmem_gb300.so; raises if it was not built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() "
+                          "(python -m gpuvmem_gb300.build)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, f32, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_double
+    f64p, f32p = C.POINTER(C.c_double), C.POINTER(C.c_float)
+    sig = {
+        "gv_problem_create": [C.POINTER(ProblemDesc), C.POINTER(vp)],
+        "gv_problem_destroy": [vp],
+        "gv_problem_info_get": [vp, C.POINTER(ProblemInfo)],
+        "gv_problem_set_stream": [vp, vp],
+        "gv_noise_image": [vp, vp],
+        "gv_initial_image": [vp, vp],
+        "gv_chi2": [vp, vp, i32, f64p],
+        "gv_dchi2": [vp, vp, i32, vp],
+        "gv_dchi2_channel": [vp, i32, vp],
+        "gv_prior_value": [vp, i32, vp, f64p],
+        "gv_prior_gradient": [vp, i32, vp, vp],
+        "gv_objective": [vp, vp, i32, f64p, f64p],
+        "gv_gradient": [vp, vp, vp, i32, i32],
+        "gv_optimize": [vp, C.POINTER(OptDesc), vp, C.POINTER(OptReport)],
+        "gv_dirty_image": [vp, vp],
+        "gv_residuals": [vp, f32p],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.gv_last_error.restype = C.c_char_p
+    L.gv_version.restype = C.c_char_p
+    _LIB = L
+    return L
+
+
+def check(status):
+    if status != GV_OK:
+        raise GvError(status, lib().gv_last_error().decode())
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def term(kind, lam, image_index=0, image_to_add=0, prior_value=0.001, eta=-1.0, epsilon=1e-12):
+    """One ObjectiveFunction term, as Fi::configure + setPrior would set it."""
+    if isinstance(kind, str):
+        kind = FI_IDS[kind]
+    return (int(kind), float(lam), int(image_index), int(image_to_add), float(prior_value),
+            float(eta), float(epsilon))
+
+
+class Problem:
+    """One imaging problem resident on the current CUDA device."""
+
+    def __init__(self, data, terms: Sequence[tuple], eta=-1.0, initial_value=0.001,
+                 noise_cut=10.0, threshold=0.0, normalize=False, engine=0, vis_noise=-1.0,
+                 stream=None):
+        L = lib()
+        self.data = data
+        self.M, self.N = data.M, data.N
+        C_ = len(data.freqs)
+        self._keep = []
+        chans = (ChannelDesc * C_)()
+        for c in range(C_):
+            o, e = int(data.chan_off[c]), int(data.chan_off[c + 1])
+            uvw = np.ascontiguousarray(data.uvw_m[o:e], dtype=np.float64)
+            vo = np.ascontiguousarray(data.vo[o:e], dtype=np.float32)
+            w = np.ascontiguousarray(data.weight[o:e], dtype=np.float32)
+            self._keep += [uvw, vo, w]
+            chans[c] = ChannelDesc(float(data.freqs[c]), e - o,
+                                   uvw.ctypes.data_as(C.POINTER(C.c_double)),
+                                   vo.ctypes.data_as(C.POINTER(C.c_float)),
+                                   w.ctypes.data_as(C.POINTER(C.c_float)))
+        tl = (FiDesc * max(1, len(terms)))()
+        for i, t in enumerate(terms):
+            tl[i] = FiDesc(*t)
+        self.terms = [t for t in terms if t[1] != 0.0]
+        desc = ProblemDesc(data.M, data.N, data.DELTAX, data.DELTAY, data.xobs, data.yobs,
+                           data.nu_0, data.antenna_diameter, data.pb_factor, data.pb_cutoff,
+                           data.primary_beam, vis_noise, noise_cut, eta, initial_value,
+                           threshold, int(normalize), C_, chans, len(terms), tl, engine)
+        h = C.c_void_p()
+        check(L.gv_problem_create(C.byref(desc), C.byref(h)))
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gv_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        check(lib().gv_problem_set_stream(self.h, C.c_void_p(stream)))
+
+    @property
+    def info(self) -> ProblemInfo:
+        inf = ProblemInfo()
+        check(lib().gv_problem_info_get(self.h, C.byref(inf)))
+        return inf
+
+    def _img(self):
+        import torch
+        return torch.zeros((2, self.N, self.M), dtype=torch.float32, device="cuda")
+
+    def initial_image(self):
+        img = self._img()
+        check(lib().gv_initial_image(self.h, _ptr(img)))
+        return img
+
+    def noise_image(self):
+        import torch
+        out = torch.empty((self.N, self.M), dtype=torch.float32, device="cuda")
+        check(lib().gv_noise_image(self.h, _ptr(out)))
+        return out
+
+    def chi2(self, img, flag_opt=0) -> float:
+        v = C.c_double()
+        check(lib().gv_chi2(self.h, _ptr(img), flag_opt, C.byref(v)))
+        return v.value
+
+    def dchi2(self, img, flag_opt=0, out=None):
+        if out is None:
+            out = self._img()
+        check(lib().gv_dchi2(self.h, _ptr(img), flag_opt, _ptr(out)))
+        return out
+
+    def dchi2_channel(self, c):
+        import torch
+        out = torch.zeros((self.N, self.M), dtype=torch.float32, device="cuda")
+        check(lib().gv_dchi2_channel(self.h, c, _ptr(out)))
+        return out
+
+    def prior_value(self, t, img) -> float:
+        v = C.c_double()
+        check(lib().gv_prior_value(self.h, t, _ptr(img), C.byref(v)))
+        return v.value
+
+    def prior_gradient(self, t, img, dphi=None):
+        if dphi is None:
+            dphi = self._img()
+        check(lib().gv_prior_gradient(self.h, t, _ptr(img), _ptr(dphi)))
+        return dphi
+
+    def objective(self, img, flag_opt=0):
+        f = C.c_double()
+        fi = (C.c_double * 8)()
+        check(lib().gv_objective(self.h, _ptr(img), flag_opt, C.byref(f), fi))
+        return f.value, list(fi)[:len(self.terms)]
+
+    def gradient(self, img, it, flag_opt=0, xi=None):
+        if xi is None:
+            xi = self._img()
+        check(lib().gv_gradient(self.h, _ptr(img), _ptr(xi), it, flag_opt))
+        return xi
+
+    def optimize(self, img, method="CG-FRPRMN", iterations=10, ftol=1e-12, gtol=1e-12, K=100,
+                 flag=0, positivity=True) -> OptReport:
+        kind = OPT_IDS[method] if isinstance(method, str) else method
+        o = OptDesc(kind, iterations, ftol, gtol, K, flag, int(positivity))
+        rep = OptReport()
+        check(lib().gv_optimize(self.h, C.byref(o), _ptr(img), C.byref(rep)))
+        return rep
+
+    def dirty_image(self):
+        import torch
+        out = torch.zeros((self.N, self.M), dtype=torch.float32, device="cuda")
+        check(lib().gv_dirty_image(self.h, _ptr(out)))
+        return out
+
+    def residuals(self) -> np.ndarray:
+        out = np.zeros((int(self.info.nvis_total), 2), dtype=np.float32)
+        check(lib().gv_residuals(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out

@@ -1,0 +1,186 @@
+// Internal declarations of the gpuvmem_gb300 library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gpuvmem_gb300.h"
+
+namespace gv {
+
+// Constants as the reference defines them (include/MSFITSIO.cuh:52-54,
+// include/functions.cuh:17-23).
+constexpr double kPiD = 3.141592653589793238462643383279502884;
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr float kLightSpeed = 2.99792458E8f;
+constexpr double kRpDegD = kPiD / 180.0;
+constexpr float kRZ = 1.2196698912665045f;
+
+// Mask byte per pixel: bit 0 = noise < noise_cut (priors, DChi2),
+// bit 1 = noise > noise_cut (clip2IWNoise).  Both are derived from the FP32
+// noise image exactly as the reference compares it.
+constexpr uint8_t kMaskIn = 1;
+constexpr uint8_t kMaskClip = 2;
+
+// Scalar slots in Problem::d_scal (FP64, device).
+enum ScalarSlot {
+  kSlotF = 0,         // objective value
+  kSlotChi2 = 1,      // chi2 (0.5 * sum)
+  kSlotTerm0 = 2,     // per-term values (up to kMaxTerms)
+  kSlotOpt = 16,      // optimiser scratch (gg, dgg, gmax, dots ...)
+  kNumScal = 64
+};
+constexpr int kMaxTerms = 8;
+
+struct Channel {
+  float freq;
+  int64_t nvis;   // visibilities of this channel (all, incl. zero weight)
+  int64_t off;    // offset into the visibility arrays
+  int64_t ngrid;  // visibilities inside the grid (weight kept)
+};
+
+struct ChanRange {
+  int64_t off;
+  int64_t ngrid;
+};
+
+struct Term {
+  int kind;
+  float lambda;
+  int image_index;
+  int image_to_add;
+  float prior_value;
+  float eta;
+  float epsilon;
+};
+
+// Packed per-visibility streams, sorted by grid cell within each channel.
+//   deg  : {cell (j1 << 16 | i1) as bits, du, dv, w}       16 B
+//   vo   : observed visibility                              8 B
+//   cvr  : w * (Vo - Vm), written by the chi2 pass          8 B
+//   ph   : {FU, FV, GU bits, GV bits} phase constants       16 B
+//          FU = frac(dx*u) * 2^32, FV = frac(dy*v) * 2^32 (exact mod 1),
+//          GU = w*dx^2/2, GV = w*dy^2/2 (cycles per pixel^2)
+//   wl   : w in wavelengths (float) for the non-separable w-term residual
+struct Problem {
+  int M = 0, N = 0, log2n = 0;
+  double DELTAX = 0, DELTAY = 0, dx_rad = 0, dy_rad = 0, deltau = 0, deltav = 0;
+  float xobs = 0, yobs = 0, nu_0 = 0, D = 0, pbf = 0, pbcut = 0;
+  int pb = 1;
+  float eta = -1, minpix = 0, threshold = 0, noise_cut = 0, fg_scale = 1;
+  int normalize = 0;
+  float vis_noise = 0, sum_weights = 0;
+  double bmaj = 0, bmin = 0, bpa = 0;
+  int64_t V = 0, Vgrid = 0, mask_pixels = 0;
+  int engine = 1;
+  double max_wrho = 0;  // bound of |w * rho| (cycles) over the data
+  std::vector<Channel> chans;
+  std::vector<Term> terms;
+
+  int iteration = 0;    // Fi::iteration of every term
+  cudaStream_t stream = 0;
+
+  // device buffers
+  float4* d_deg = nullptr;
+  float2* d_vo = nullptr;
+  float2* d_cvr = nullptr;
+  uint4* d_ph = nullptr;
+  float* d_wl = nullptr;
+  int64_t* d_perm = nullptr;     // sorted position -> caller's index
+  float* d_noise = nullptr;      // [MN]
+  uint8_t* d_mask = nullptr;     // [MN]
+  float* d_rho = nullptr;        // [MN] z - 1 + r^2/2 per pixel
+  float2* d_grid = nullptr;      // [C][MN] model grids
+  float2* d_twiddle = nullptr;   // [n/2] e^{+2 pi i k/n}
+  double* d_part = nullptr;      // reduction partials
+  int part_stride = 0;           // partials per channel / term
+  double* d_scal = nullptr;      // [kNumScal]
+  double* h_scal = nullptr;      // pinned mirror
+  float* d_tmp = nullptr;        // [2*MN] scratch image (dchi2 channel etc.)
+  float* d_opt = nullptr;        // optimiser workspace (allocated on demand)
+  size_t opt_bytes = 0;
+  float* d_lbfgs = nullptr;      // L-BFGS s/y rings
+  size_t lbfgs_bytes = 0;
+  float* d_chfreq = nullptr;     // [C] channel frequencies
+  ChanRange* d_ranges = nullptr; // [C] kept-visibility ranges
+  int64_t* d_chnvis = nullptr;   // [C] visibilities per channel (normalize)
+  int num_sms = 0;
+};
+
+// error state
+void set_error(const std::string& msg);
+gv_status cuda_fail(cudaError_t e, const char* what);
+
+#define GV_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return ::gv::cuda_fail(_e, #call); \
+  } while (0)
+
+#define GV_LAUNCH(what)                                         \
+  do {                                                          \
+    cudaError_t _e = cudaGetLastError();                        \
+    if (_e != cudaSuccess) return ::gv::cuda_fail(_e, what);     \
+  } while (0)
+
+// ---- device helpers shared by several translation units ---------------
+
+// freq_to_wavelength, src/MSFITSIO.cu:36-39 (float)
+__host__ __device__ inline float wavelength(float freq) { return kLightSpeed / freq; }
+
+// attenuation(), src/functions.cu:2304-2333, with the Gaussian and Airy
+// beams of :2275-2302; float arithmetic as the reference.
+__device__ inline float attenuation(int i, int j, float xobs, float yobs,
+                                    double DELTAX, double DELTAY, float freq,
+                                    float D, float pbf, float cutoff, int pb) {
+  const int x0 = (int)xobs, y0 = (int)yobs;
+  const float x = (float)((j - x0) * DELTAX * kRpDegD);
+  const float y = (float)((i - y0) * DELTAY * kRpDegD);
+  const float arc = sqrtf(x * x + y * y);
+  const float lambda = wavelength(freq);
+  float atten;
+  if (pb == GV_BEAM_GAUSSIAN) {
+    const float fwhm = pbf * lambda / D;
+    const float c = 4.0f * logf(2.0f);
+    const float r = arc / fwhm;
+    atten = expf(-c * r * r);
+  } else {
+    atten = 1.0f;
+    if (arc != 0.0f) {
+      const float arg = kPiF * arc * D / lambda * (kRZ / pbf);
+      const float b = j1f(arg);
+      atten = 4.0f * (b / arg) * (b / arg);
+    }
+  }
+  return arc <= cutoff ? atten : 0.0f;
+}
+
+// ---- entry points between translation units ----------------------------
+gv_status setup_problem(Problem& P, const gv_problem_desc& d);
+void free_problem(Problem& P);
+
+// objective.cu
+gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot);
+gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi);
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+gv_status fetch_scalars(Problem& P, int n);
+gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
+gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);
+gv_status gradient_launch(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt);
+gv_status dirty_launch(Problem& P, float* d_out);
+
+// dchi2 engines
+gv_status dchi2_direct(Problem& P, const float* d_img, int flag_opt, float* d_result,
+                       int only_channel, int mode);
+gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result,
+                   int only_channel, int mode);
+bool dchi2_tc_supported(const Problem& P);
+
+// optimiser
+gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep);
+
+}  // namespace gv

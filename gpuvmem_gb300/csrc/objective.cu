@@ -1,0 +1,510 @@
+// Objective function on the GPU: chi2() (src/functions.cu:4323-4454) and the
+// prior values/gradients (src/functions.cu:2878-3545,4633-4964), arranged
+// as three passes per evaluation over all channels at once:
+//
+//   1. k_rows_fft   clip2IWNoise + calculateInu + apply_beam2I staged
+//                   straight into shared memory, then the row pass of the
+//                   2-D C2C inverse FFT (cuFFT CUFFT_INVERSE convention:
+//                   unnormalised, exp(+i));
+//   2. k_cols_fft   column pass of the FFT, with phase_rotate applied on the
+//                   way out;
+//   3. k_degrid     vis_mod + residual + chi2Vector + reduction: one stream
+//                   over the cell-sorted visibilities, FP64 partial sums,
+//                   weighted residuals stored for DChi2.
+//
+// No per-call allocation, no host synchronisation except the single scalar
+// read-back at the end of an evaluation.
+#include <cmath>
+
+#include "gv_internal.cuh"
+
+namespace gv {
+
+namespace {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ unsigned bitrev(unsigned x, int bits) {
+  return __brev(x) >> (32 - bits);
+}
+
+// In-place inverse radix-2 DIT FFT of `ncol` independent columns of length
+// n = 2^log2n held in shared memory (column c at buf + c*n), input in
+// bit-reversed order, output in natural order.
+__device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restrict__ tw) {
+  const int n = 1 << log2n;
+  const int nb = (n >> 1) * ncol;
+  for (int s = 1; s <= log2n; s++) {
+    const int half = 1 << (s - 1);
+    const int tstride = n >> s;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      const int col = b >> (log2n - 1);
+      const int bb = b & ((n >> 1) - 1);
+      const int grp = bb >> (s - 1);
+      const int pos = bb & (half - 1);
+      const int a0 = col * n + (grp << s) + pos;
+      const int a1 = a0 + half;
+      const float2 w = tw[pos * tstride];
+      const float2 t = cmul(w, buf[a1]);
+      const float2 x0 = buf[a0];
+      buf[a0] = make_float2(x0.x + t.x, x0.y + t.y);
+      buf[a1] = make_float2(x0.x - t.x, x0.y - t.y);
+    }
+    __syncthreads();
+  }
+}
+
+struct StageParams {
+  int M, N, log2n;
+  int64_t MN;
+  float xobs, yobs, nu_0, D, pbf, pbcut;
+  int pb;
+  double DELTAX, DELTAY;
+  float eta, minpix, threshold, fg_scale;
+  int flag_opt;
+  int write_clip;
+};
+
+// Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
+__global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
+                           float* __restrict__ img, const uint8_t* __restrict__ mask,
+                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
+  extern __shared__ float2 sm[];
+  const int n = sp.N;
+  float2* buf = sm;
+  float2* tw = sm + n;
+  const int i = blockIdx.x;
+  const int c = blockIdx.y;
+  for (int k = threadIdx.x; k < n / 2; k += blockDim.x) tw[k] = tw_g[k];
+  const float freq = chfreq[c];
+  const float nudiv = freq / sp.nu_0;
+  const float floor_inu = -1.0f * sp.eta * sp.minpix;
+  const float clip_i0 = sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix);
+  const bool writer = sp.write_clip && c == 0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int64_t q = (int64_t)n * i + j;
+    float i0 = img[q];
+    float al = img[sp.MN + q];
+    const uint8_t m = mask[q];
+    // clip2IWNoise, src/functions.cu:2694-2719 (mutates the image)
+    if (m & kMaskClip) {
+      if (writer && (i0 != clip_i0 || al != 0.0f)) {
+        img[q] = clip_i0;
+        img[sp.MN + q] = 0.0f;
+      }
+      i0 = clip_i0;
+      al = 0.0f;
+    } else if (i0 < sp.threshold && sp.flag_opt > 0) {
+      if (writer && al != 0.0f) img[sp.MN + q] = 0.0f;
+      al = 0.0f;
+    }
+    // calculateInu, src/functions.cu:3939-3966
+    float inu = i0 * powf(nudiv, al);
+    if (inu < floor_inu) inu = floor_inu;
+    // apply_beam2I, src/functions.cu:2424-2444
+    const float a = attenuation(i, j, sp.xobs, sp.yobs, sp.DELTAX, sp.DELTAY, freq, sp.D,
+                                sp.pbf, sp.pbcut, sp.pb);
+    buf[bitrev(j, sp.log2n)] = make_float2(inu * a * sp.fg_scale, 0.0f);
+  }
+  __syncthreads();
+  smem_fft(buf, sp.log2n, 1, tw);
+  float2* out = grid + (int64_t)c * sp.MN + (int64_t)n * i;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[j];
+}
+
+// Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate
+// (src/functions.cu:2483-2518) in the reference's float arithmetic.
+__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, float xphs, float yphs,
+                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
+  extern __shared__ float2 sm[];
+  const int n = N;
+  float2* buf = sm;
+  float2* tw = sm + (size_t)cb * n;
+  const int j0 = blockIdx.x * cb;
+  float2* G = grid + (int64_t)blockIdx.y * MN;
+  for (int k = threadIdx.x; k < n / 2; k += blockDim.x) tw[k] = tw_g[k];
+  for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
+    const int r = idx / cb, cc = idx - r * cb;
+    buf[cc * n + bitrev(r, log2n)] = G[(int64_t)n * r + j0 + cc];
+  }
+  __syncthreads();
+  smem_fft(buf, log2n, cb, tw);
+  const double upix = (double)xphs / (double)n;
+  const double vpix = (double)yphs / (double)n;
+  for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
+    const int r = idx / cb, cc = idx - r * cb;
+    const int j = j0 + cc;
+    const float u = (float)(j < n / 2 ? upix * j : upix * (j - n));
+    const float v = (float)(r < n / 2 ? vpix * r : vpix * (r - n));
+    const float phase = -2.0f * (u + v);
+    float s, co;
+    sincospif(phase, &s, &co);
+    G[(int64_t)n * r + j] = cmul(buf[cc * n + r], make_float2(co, s));
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide FP64 sum; result valid in thread 0
+__device__ double block_sum(double v) {
+  __shared__ double red[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = threadIdx.x < nw ? red[threadIdx.x] : 0.0;
+  if (wid == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;
+}
+
+// Pass 3: vis_mod + residual + chi2Vector + partial reduction.
+__global__ void __launch_bounds__(256) k_degrid(
+    int N, int64_t MN, const ChanRange* __restrict__ ranges,
+    const float4* __restrict__ deg, const float2* __restrict__ vo,
+    const float2* __restrict__ grid, float2* __restrict__ cvr, int store,
+    double* __restrict__ part, int part_stride) {
+  const int c = blockIdx.y;
+  const ChanRange rg = ranges[c];
+  const float2* __restrict__ G = grid + (int64_t)c * MN;
+  const int nm1 = N - 1;
+  double acc = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const float4 d = __ldcs(deg + rg.off + k);
+    const float2 o = __ldcs(vo + rg.off + k);
+    const uint32_t cell = __float_as_uint(d.x);
+    const int i1 = cell & 0xffff, j1 = cell >> 16;
+    const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
+    const float2 v11 = __ldg(G + (int64_t)N * j1 + i1);
+    const float2 v12 = __ldg(G + (int64_t)N * j2 + i1);
+    const float2 v21 = __ldg(G + (int64_t)N * j1 + i2);
+    const float2 v22 = __ldg(G + (int64_t)N * j2 + i2);
+    const float du = d.y, dv = d.z;
+    const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
+    const float w21 = du * (1.0f - dv), w22 = du * dv;
+    const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
+    const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
+    const float rr = o.x - mr, ri = o.y - mi;
+    acc += (double)(d.w * (rr * rr + ri * ri));
+    if (store) __stcs(cvr + rg.off + k, make_float2(d.w * rr, d.w * ri));
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = acc;
+}
+
+// Sum of channel partials in a fixed order; writes 0.5 * sum to out.
+__global__ void k_finish_chi2(int C, int nb, const double* __restrict__ part, int part_stride,
+                              const int64_t* __restrict__ nvis, int normalize,
+                              double* __restrict__ out) {
+  __shared__ double tot;
+  if (threadIdx.x == 0) tot = 0.0;
+  __syncthreads();
+  for (int c = 0; c < C; c++) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[(int64_t)c * part_stride + b];
+    v = block_sum(v);
+    if (threadIdx.x == 0) {
+      if (normalize && nvis[c] > 0) v /= (double)nvis[c];
+      tot += v;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = 0.5 * tot;
+}
+
+__global__ void k_finish_sum(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[b];
+  v = block_sum(v);
+  if (threadIdx.x == 0) *out = v;
+}
+
+// ---- priors ---------------------------------------------------------------
+
+struct PriorParams {
+  int kind;
+  int N;
+  int64_t MN;
+  float lambda, G, eta, eps;
+};
+
+// Value of one pixel, src/functions.cu:2882 (L1), 3036 (S), 3238 (TV),
+// 3353 (TSV), 3443 (L); the caller has checked the mask.
+__device__ __forceinline__ float prior_pixel(const PriorParams& pp, const float* __restrict__ I,
+                                             int i, int j) {
+  const int N = pp.N;
+  const float c = I[(int64_t)N * i + j];
+  switch (pp.kind) {
+    case GV_FI_ENTROPY:
+      return c * logf((c / pp.G) + (pp.eta + 1.0f));
+    case GV_FI_L1:
+      return sqrtf(c * c + pp.eps);
+    case GV_FI_TSV:
+      if (i < N - 1 && j < N - 1) {
+        const float dx = c - I[(int64_t)N * i + j + 1];
+        const float dy = c - I[(int64_t)N * (i + 1) + j];
+        return dx * dx + dy * dy;
+      }
+      return c;
+    case GV_FI_TV:
+      if (i < N - 1 && j < N - 1) {
+        const float r = I[(int64_t)N * i + j + 1];
+        const float d = I[(int64_t)N * (i + 1) + j];
+        return sqrtf((r - c) * (r - c) + (d - c) * (d - c) + pp.eps);
+      }
+      return c;
+    case GV_FI_LAPLACIAN:
+      if (i > 0 && i < N - 1 && j > 0 && j < N - 1) {
+        const float Dx = I[(int64_t)N * i + j - 1] - 2.0f * c + I[(int64_t)N * i + j + 1];
+        const float Dy = I[(int64_t)N * (i - 1) + j] - 2.0f * c + I[(int64_t)N * (i + 1) + j];
+        return 0.5f * (Dx + Dy) * (Dx + Dy);
+      }
+      return c;
+  }
+  return 0.0f;
+}
+
+// Gradient of one pixel before lambda, src/functions.cu:2917 (DL1), 3057
+// (DS), 3284 (DTV), 3395 (DTSV), 3488 (DL, with its d - r - u - l sign).
+__device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
+                                                  const float* __restrict__ I, int i, int j) {
+  const int N = pp.N;
+  const float c = I[(int64_t)N * i + j];
+  const bool inner = i > 0 && i < N - 1 && j > 0 && j < N - 1;
+#define P_(r, cc) I[(int64_t)N * (r) + (cc)]
+  switch (pp.kind) {
+    case GV_FI_ENTROPY:
+      return logf((c / pp.G) + (pp.eta + 1.0f)) + 1.0f / (1.0f + (((pp.eta + 1.0f) * pp.G) / c));
+    case GV_FI_L1:
+      return c / sqrtf(c * c + pp.eps);
+    case GV_FI_TSV:
+      if (inner) return 8.0f * c - 2.0f * (P_(i - 1, j) + P_(i, j - 1) + P_(i + 1, j) + P_(i, j + 1));
+      return c;
+    case GV_FI_TV:
+      if (inner) {
+        const float d = P_(i + 1, j), u = P_(i - 1, j), r = P_(i, j + 1), l = P_(i, j - 1);
+        const float dl = P_(i + 1, j - 1), ru = P_(i - 1, j + 1);
+        const float num0 = 2.0f * c - r - d, num1 = c - l, num2 = c - u;
+        const float den0 = sqrtf((c - r) * (c - r) + (c - d) * (c - d) + pp.eps);
+        const float den1 = sqrtf((l - c) * (l - c) + (l - dl) * (l - dl) + pp.eps);
+        const float den2 = sqrtf((u - ru) * (u - ru) + (u - c) * (u - c) + pp.eps);
+        return num0 / den0 + num1 / den1 + num2 / den2;
+      }
+      return c;
+    case GV_FI_LAPLACIAN:
+      if (i > 1 && i < N - 2 && j > 1 && j < N - 2) {
+        return 20.0f * c - 8.0f * (P_(i + 1, j) - P_(i, j + 1) - P_(i - 1, j) - P_(i, j - 1)) +
+               2.0f * (P_(i + 1, j - 1) + P_(i + 1, j + 1) + P_(i - 1, j - 1) + P_(i - 1, j + 1)) +
+               P_(i + 2, j) + P_(i, j + 2) + P_(i - 2, j) + P_(i, j - 2);
+      }
+      return 0.0f;
+  }
+#undef P_
+  return 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_prior_value(PriorParams pp, const float* __restrict__ I,
+                                                     const uint8_t* __restrict__ mask,
+                                                     double* __restrict__ part) {
+  double acc = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    if (!(mask[q] & kMaskIn)) continue;
+    const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
+    acc += (double)prior_pixel(pp, I, i, j);
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float* __restrict__ I,
+                                                    const uint8_t* __restrict__ mask,
+                                                    float* __restrict__ dphi) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    if (!(mask[q] & kMaskIn)) continue;
+    const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
+    const float g = prior_grad_pixel(pp, I, i, j) * pp.lambda;
+    dphi[q] += g;  // AddToDPhi, src/functions.cu:3890
+  }
+}
+
+}  // namespace
+
+static int cols_per_block(int n) {
+  int cb = 16384 / n;
+  if (cb < 1) cb = 1;
+  if (cb > 16) cb = 16;
+  return cb;
+}
+
+// Model grids of all channels for image d_img (clip written back when
+// write_clip).
+gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_clip) {
+  const int n = P.N, C = (int)P.chans.size();
+  StageParams sp;
+  sp.M = P.M;
+  sp.N = P.N;
+  sp.log2n = P.log2n;
+  sp.MN = (int64_t)P.M * P.N;
+  sp.xobs = P.xobs;
+  sp.yobs = P.yobs;
+  sp.nu_0 = P.nu_0;
+  sp.D = P.D;
+  sp.pbf = P.pbf;
+  sp.pbcut = P.pbcut;
+  sp.pb = P.pb;
+  sp.DELTAX = P.DELTAX;
+  sp.DELTAY = P.DELTAY;
+  sp.eta = P.eta;
+  sp.minpix = P.minpix;
+  sp.threshold = P.threshold;
+  sp.fg_scale = P.fg_scale;
+  sp.flag_opt = flag_opt;
+  sp.write_clip = write_clip;
+  const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
+  const size_t sm1 = sizeof(float2) * (n + n / 2);
+  if (sm1 > 48 * 1024)
+    GV_CUDA(cudaFuncSetAttribute(k_rows_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
+  k_rows_fft<<<dim3(n, C), threads, sm1, P.stream>>>(sp, P.d_chfreq, d_img, P.d_mask, P.d_twiddle,
+                                                     P.d_grid);
+  GV_LAUNCH("k_rows_fft");
+  const int cb = cols_per_block(n);
+  const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n / 2);
+  if (sm2 > 48 * 1024)
+    GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+  k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.xobs, P.yobs,
+                                                      P.d_twiddle, P.d_grid);
+  GV_LAUNCH("k_cols_fft");
+  return GV_OK;
+}
+
+gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
+  gv_status s = model_grids_launch(P, d_img, flag_opt, 1);
+  if (s != GV_OK) return s;
+  const int C = (int)P.chans.size();
+  int64_t maxg = 1;
+  for (auto& ch : P.chans) maxg = std::max<int64_t>(maxg, ch.ngrid);
+  int nb = (int)std::min<int64_t>((maxg + 255) / 256, P.part_stride);
+  if (nb < 1) nb = 1;
+  const int64_t MN = (int64_t)P.M * P.N;
+  k_degrid<<<dim3(nb, C), 256, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
+                                              P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride);
+  GV_LAUNCH("k_degrid");
+  k_finish_chi2<<<1, 256, 0, P.stream>>>(C, nb, P.d_part, P.part_stride, P.d_chnvis, P.normalize,
+                                         P.d_scal + kSlotChi2);
+  GV_LAUNCH("k_finish_chi2");
+  return GV_OK;
+}
+
+static PriorParams prior_params(const Problem& P, const Term& t) {
+  PriorParams pp;
+  pp.kind = t.kind;
+  pp.N = P.N;
+  pp.MN = (int64_t)P.M * P.N;
+  pp.lambda = t.lambda;
+  pp.G = t.prior_value;
+  pp.eta = t.eta;
+  pp.eps = t.epsilon;
+  return pp;
+}
+
+gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot) {
+  const Term& tm = P.terms[t];
+  PriorParams pp = prior_params(P, tm);
+  const int64_t MN = pp.MN;
+  int nb = (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
+  double* part = P.d_part + (int64_t)P.part_stride * (P.chans.size() + t);
+  k_prior_value<<<nb, 256, 0, P.stream>>>(pp, d_img + MN * tm.image_index, P.d_mask, part);
+  GV_LAUNCH("k_prior_value");
+  k_finish_sum<<<1, 256, 0, P.stream>>>(nb, part, P.d_scal + slot);
+  GV_LAUNCH("k_finish_sum");
+  return GV_OK;
+}
+
+gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi) {
+  const Term& tm = P.terms[t];
+  PriorParams pp = prior_params(P, tm);
+  const int64_t MN = pp.MN;
+  // TVariation::addToDphi adds into plane 0 whatever imageToAdd is
+  // (src/totalvariation.cu:48)
+  const int add = tm.kind == GV_FI_TV ? 0 : tm.image_to_add;
+  int nb = (int)std::min<int64_t>((MN + 255) / 256, 8 * P.num_sms);
+  k_prior_grad<<<nb, 256, 0, P.stream>>>(pp, d_img + MN * tm.image_index, P.d_mask,
+                                         d_dphi + MN * add);
+  GV_LAUNCH("k_prior_grad");
+  return GV_OK;
+}
+
+// ObjectiveFunction::calcFunction; values land in d_scal[kSlotTerm0 + t].
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    const Term& tm = P.terms[t];
+    gv_status s = GV_OK;
+    if (tm.kind == GV_FI_CHI2) {
+      s = chi2_launch(P, d_img, flag_opt, store_res);
+      if (s == GV_OK) {
+        GV_CUDA(cudaMemcpyAsync(P.d_scal + kSlotTerm0 + t, P.d_scal + kSlotChi2, sizeof(double),
+                                cudaMemcpyDeviceToDevice, P.stream));
+      }
+    } else if (P.iteration > 0 && tm.lambda != 0.0f) {
+      s = prior_value_launch(P, (int)t, d_img, kSlotTerm0 + (int)t);
+    } else {
+      GV_CUDA(cudaMemsetAsync(P.d_scal + kSlotTerm0 + t, 0, sizeof(double), P.stream));
+    }
+    if (s != GV_OK) return s;
+  }
+  return GV_OK;
+}
+
+gv_status fetch_scalars(Problem& P, int n) {
+  GV_CUDA(cudaMemcpyAsync(P.h_scal, P.d_scal, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                          P.stream));
+  GV_CUDA(cudaStreamSynchronize(P.stream));
+  return GV_OK;
+}
+
+gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result) {
+  if (P.engine == 2) return dchi2_tc(P, d_img, flag_opt, d_result, -1, 0);
+  return dchi2_direct(P, d_img, flag_opt, d_result, -1, 0);
+}
+
+gv_status dchi2_channel_launch(Problem& P, int c, float* d_out) {
+  GV_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * P.M * P.N, P.stream));
+  if (P.engine == 2) return dchi2_tc(P, nullptr, 0, d_out, c, 1);
+  return dchi2_direct(P, nullptr, 0, d_out, c, 1);
+}
+
+gv_status dirty_launch(Problem& P, float* d_out) {
+  GV_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * P.M * P.N, P.stream));
+  if (P.engine == 2) return dchi2_tc(P, nullptr, 0, d_out, -1, 2);
+  return dchi2_direct(P, nullptr, 0, d_out, -1, 2);
+}
+
+// ObjectiveFunction::calcGradient (include/classes/objectivefunction.cuh:28-57)
+gv_status gradient_launch(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt) {
+  const int64_t MN = (int64_t)P.M * P.N;
+  P.iteration = iter;  // setIteration(iter) on every Fi
+  GV_CUDA(cudaMemsetAsync(d_xi, 0, sizeof(float) * 2 * MN, P.stream));
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    const Term& tm = P.terms[t];
+    gv_status s = GV_OK;
+    if (tm.kind == GV_FI_CHI2) {
+      s = dchi2_launch(P, d_img, flag_opt, d_xi);
+    } else if (iter > 0 && tm.lambda != 0.0f && (flag_opt % 2) == tm.image_index) {
+      s = prior_grad_launch(P, (int)t, d_img, d_xi);
+    }
+    if (s != GV_OK) return s;
+  }
+  return GV_OK;
+}
+
+}  // namespace gv

@@ -1,0 +1,643 @@
+// Optimisers of the reference's Optimizer surface on the GPU:
+//   "CG-FRPRMN"  ConjugateGradient::optimize   src/frprmn.cu:85-195
+//   "CG-LBFGS"   LBFGS::optimize + recursion  src/lbfgs.cu:99-341
+// with linmin / f1dim (src/linmin.cu:52-110, src/f1dim.cu:49-80) and the
+// bracketing and Brent line minimisers (src/mnbrak.cu:44-98,
+// src/brent.cu:43-121; the published algorithms of Brent 1973 with the
+// reference's constants).  Host scalars are float, as in the reference, so
+// the line search takes the same decisions; vector updates are fused GPU
+// kernels and all dot products and reductions accumulate in FP64.
+//
+// L-BFGS keeps the reference's ring addressing: getDot_LBFGS_ff and
+// calculateSandY use slot offset M*N*image*k + M*N*image, updateQ uses
+// M*N*image + M*N*k (src/functions.cu:3571-3653).
+#include <algorithm>
+#include <chrono>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "gv_internal.cuh"
+
+namespace gv {
+
+namespace {
+
+// GV_VERBOSE=1 prints the line-search and iteration values, as the
+// reference's --verbose flag does (src/linmin.cu:83, src/frprmn.cu:131).
+bool verbose() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("GV_VERBOSE");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// evaluateXt / evaluateXtNoPositivity, src/functions.cu:2832-2864
+__global__ void k_eval_xt(int64_t MN, float x, float floor_val, double floor_cmp,
+                          int positivity, const float* __restrict__ pcom,
+                          const float* __restrict__ xicom, float* __restrict__ xt) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= 2 * MN) return;
+  const float v = fmaf(x, xicom[q], pcom[q]);
+  xt[q] = (q < MN && positivity && !((double)v > floor_cmp)) ? floor_val : v;
+}
+
+// newP / newPNoPositivity, src/functions.cu:2779-2812
+__global__ void k_new_p(int64_t MN, float xmin, float floor_val, double floor_cmp,
+                        int positivity, float* __restrict__ p, float* __restrict__ xi) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= 2 * MN) return;
+  const float s = xi[q] * xmin;
+  if (q < MN && positivity) {
+    if ((double)(p[q] + s) > floor_cmp) {
+      p[q] += s;
+      xi[q] = s;
+    } else {
+      p[q] = floor_val;
+      xi[q] = 0.0f;
+    }
+  } else {
+    xi[q] = s;
+    p[q] += s;
+  }
+}
+
+// searchDirection, src/functions.cu:3655
+__global__ void k_cg_init(int64_t n, float* __restrict__ g, float* __restrict__ xi,
+                          float* __restrict__ h) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float v = -xi[q];
+  g[q] = v;
+  xi[q] = v;
+  h[q] = v;
+}
+
+// newXi, src/functions.cu:3678
+__global__ void k_new_xi(int64_t n, float gam, float* __restrict__ g, float* __restrict__ xi,
+                         float* __restrict__ h) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float gv = -xi[q];
+  const float hv = fmaf(gam, h[q], gv);
+  g[q] = gv;
+  xi[q] = hv;
+  h[q] = hv;
+}
+
+// CGGradCondition + deviceMaxReduce and getGGandDGG + 2 deviceReduce of
+// frprmn (src/frprmn.cu:137-168) fused into one pass: partials of
+// gmax = max |xi| max(|p|,1)/den, gg = sum g^2, dgg = sum (xi+g) xi.
+__global__ void __launch_bounds__(256) k_cg_stats(int64_t n, float den,
+                                                  const float* __restrict__ xi,
+                                                  const float* __restrict__ g,
+                                                  const float* __restrict__ p,
+                                                  double* __restrict__ part, int stride) {
+  double gg = 0.0, dgg = 0.0;
+  float gmax = FLT_MIN;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const float x = xi[q], gq = g[q];
+    gmax = fmaxf(gmax, fabsf(x) * fmaxf(fabsf(p[q]), 1.0f) / den);
+    gg += (double)(gq * gq);
+    dgg += (double)((x + gq) * x);
+  }
+  __shared__ double s1[32], s2[32];
+  __shared__ float s3[32];
+  gg = warp_sum_d(gg);
+  dgg = warp_sum_d(dgg);
+  gmax = warp_max_f(gmax);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    s1[wid] = gg;
+    s2[wid] = dgg;
+    s3[wid] = gmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    float m = FLT_MIN;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      a += s1[w];
+      b += s2[w];
+      m = fmaxf(m, s3[w]);
+    }
+    part[blockIdx.x] = a;
+    part[stride + blockIdx.x] = b;
+    part[2 * stride + blockIdx.x] = (double)m;
+  }
+}
+
+__global__ void k_cg_finish(int nb, const double* __restrict__ part, int stride,
+                            double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double a = 0.0, b = 0.0, m = (double)FLT_MIN;
+  for (int i = 0; i < nb; i++) {
+    a += part[i];
+    b += part[stride + i];
+    m = fmax(m, part[2 * stride + i]);
+  }
+  out[0] = a;
+  out[1] = b;
+  out[2] = m;
+}
+
+// FP64 dot product partials of two float vectors
+__global__ void __launch_bounds__(256) k_dot(int64_t n, const float* __restrict__ a,
+                                             const float* __restrict__ b,
+                                             double* __restrict__ part) {
+  double s = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    s += (double)(a[q] * b[q]);
+  __shared__ double sh[32];
+  s = warp_sum_d(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_sum_partials(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < nb; i++) t += part[i];
+    *out = t;
+  }
+}
+
+// max |x| (normArray + deviceMaxReduce, seeded with FLT_MIN)
+__global__ void __launch_bounds__(256) k_absmax(int64_t n, const float* __restrict__ x,
+                                                double* __restrict__ part) {
+  float m = FLT_MIN;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[q]));
+  __shared__ float sh[32];
+  m = warp_max_f(m);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = FLT_MIN;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmaxf(t, sh[w]);
+    part[blockIdx.x] = (double)t;
+  }
+}
+
+__global__ void k_max_partials(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double t = (double)FLT_MIN;
+    for (int i = 0; i < nb; i++) t = fmax(t, part[i]);
+    *out = t;
+  }
+}
+
+__global__ void k_scale(int64_t n, float a, float* __restrict__ x) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < n) x[q] *= a;
+}
+
+// y := a*x + y  (updateQ, src/functions.cu:3614, contracted to an FMA)
+__global__ void k_axpy(int64_t n, float a, const float* __restrict__ x, float* __restrict__ y) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < n) y[q] = fmaf(a, x[q], y[q]);
+}
+
+// r := q * s  (getR)
+__global__ void k_scaled_copy(int64_t n, float s, const float* __restrict__ q,
+                              float* __restrict__ r) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) r[k] = q[k] * s;
+}
+
+// calculateSandY for one plane, src/functions.cu:3635
+__global__ void k_s_and_y(int64_t n, const float* __restrict__ xi, const float* __restrict__ xi_old,
+                          const float* __restrict__ p, const float* __restrict__ p_old,
+                          float* __restrict__ y, float* __restrict__ s) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  y[q] = xi[q] - (-1.0f * xi_old[q]);
+  s[q] = p[q] - p_old[q];
+}
+
+inline unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+// SIGN of include/nrutil.h:55 on float magnitudes
+inline float signf(float a, float b) { return b >= 0.0 ? std::fabs(a) : -std::fabs(a); }
+
+struct Workspace {
+  float *pcom, *xicom, *xt, *xi, *g, *h, *xi_old, *p_old, *q, *r;
+};
+
+class Solver {
+ public:
+  Solver(Problem& P, const gv_opt_desc& o) : P_(P), o_(o) {
+    MN_ = (int64_t)P.M * P.N;
+    floor_val_ = -1.0f * P.eta * P.minpix;
+    floor_cmp_ = -1.0 * P.eta * P.minpix;
+  }
+
+  gv_status init() {
+    const size_t need = sizeof(float) * 2 * MN_ * 10;
+    if (P_.opt_bytes < need) {
+      cudaFree(P_.d_opt);
+      P_.d_opt = nullptr;
+      P_.opt_bytes = 0;
+      GV_CUDA(cudaMalloc(&P_.d_opt, need));
+      P_.opt_bytes = need;
+    }
+    float* b = P_.d_opt;
+    const int64_t s = 2 * MN_;
+    w_ = Workspace{b, b + s, b + 2 * s, b + 3 * s, b + 4 * s, b + 5 * s,
+                   b + 6 * s, b + 7 * s, b + 8 * s, b + 9 * s};
+    GV_CUDA(cudaMemsetAsync(P_.d_opt, 0, need, P_.stream));
+    if (o_.kind == GV_OPT_LBFGS) {
+      const size_t ring = sizeof(float) * (size_t)MN_ * o_.K * 2;
+      if (P_.lbfgs_bytes < 2 * ring) {
+        cudaFree(P_.d_lbfgs);
+        P_.d_lbfgs = nullptr;
+        P_.lbfgs_bytes = 0;
+        GV_CUDA(cudaMalloc(&P_.d_lbfgs, 2 * ring));
+        P_.lbfgs_bytes = 2 * ring;
+      }
+      d_y_ = P_.d_lbfgs;
+      d_s_ = P_.d_lbfgs + (size_t)MN_ * o_.K * 2;
+      GV_CUDA(cudaMemsetAsync(P_.d_lbfgs, 0, 2 * ring, P_.stream));
+    }
+    return GV_OK;
+  }
+
+  // ObjectiveFunction::calcFunction as float (the reference's return type)
+  gv_status func(float* img, bool store_res, float* out) {
+    gv_status s = objective_launch(P_, img, o_.flag, store_res);
+    if (s != GV_OK) return s;
+    s = fetch_scalars(P_, kSlotTerm0 + (int)P_.terms.size());
+    if (s != GV_OK) return s;
+    double f = 0.0;
+    for (size_t t = 0; t < P_.terms.size(); t++)
+      f += (double)P_.terms[t].lambda * P_.h_scal[kSlotTerm0 + t];
+    n_obj_++;
+    *out = (float)f;
+    return GV_OK;
+  }
+
+  gv_status grad(float* img, float* xi, int iter) {
+    n_grad_++;
+    return gradient_launch(P_, img, xi, iter, o_.flag);
+  }
+
+  // f1dim: xt = pcom + x*xicom (floored on plane 0), then the objective.
+  gv_status f1dim(float x, float* out) {
+    k_eval_xt<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, x, floor_val_, floor_cmp_,
+                                                     o_.positivity, w_.pcom, w_.xicom, w_.xt);
+    GV_LAUNCH("k_eval_xt");
+    return func(w_.xt, false, out);
+  }
+
+#define GV_TRY(expr)                 \
+  do {                               \
+    gv_status _s = (expr);           \
+    if (_s != GV_OK) return _s;      \
+  } while (0)
+
+  // Bracketing of a minimum along the line (golden-section steps with
+  // parabolic extrapolation); constants of src/mnbrak.cu:35-37.
+  gv_status bracket(float* ax, float* bx, float* cx, float* fa, float* fb, float* fc) {
+    const double gold = 1.618034, glimit = 100.0, tiny = 1.0e-20;
+    GV_TRY(f1dim(*ax, fa));
+    GV_TRY(f1dim(*bx, fb));
+    if (*fb > *fa) {
+      std::swap(*ax, *bx);
+      std::swap(*fa, *fb);
+    }
+    *cx = (float)(*bx + gold * (*bx - *ax));
+    GV_TRY(f1dim(*cx, fc));
+    while (*fb > *fc) {
+      const float r = (*bx - *ax) * (*fb - *fc);
+      const float q = (*bx - *cx) * (*fb - *fa);
+      const float aq = std::fabs(q - r), at = (float)tiny;
+      const float den = aq > at ? aq : at;
+      float u = (float)(*bx - ((*bx - *cx) * q - (*bx - *ax) * r) / (2.0 * signf(den, q - r)));
+      const float ulim = (float)(*bx + glimit * (*cx - *bx));
+      float fu;
+      if ((*bx - u) * (u - *cx) > 0.0) {
+        GV_TRY(f1dim(u, &fu));
+        if (fu < *fc) {
+          *ax = *bx;
+          *bx = u;
+          *fa = *fb;
+          *fb = fu;
+          return GV_OK;
+        } else if (fu > *fb) {
+          *cx = u;
+          *fc = fu;
+          return GV_OK;
+        }
+        u = (float)(*cx + gold * (*cx - *bx));
+        GV_TRY(f1dim(u, &fu));
+      } else if ((*cx - u) * (u - ulim) > 0.0) {
+        GV_TRY(f1dim(u, &fu));
+        if (fu < *fc) {
+          *bx = *cx;
+          *cx = u;
+          u = (float)(*cx + gold * (*cx - *bx));
+          *fb = *fc;
+          *fc = fu;
+          GV_TRY(f1dim(u, &fu));
+        }
+      } else if ((u - ulim) * (ulim - *cx) >= 0.0) {
+        u = ulim;
+        GV_TRY(f1dim(u, &fu));
+      } else {
+        u = (float)(*cx + gold * (*cx - *bx));
+        GV_TRY(f1dim(u, &fu));
+      }
+      *ax = *bx;
+      *bx = *cx;
+      *cx = u;
+      *fa = *fb;
+      *fb = *fc;
+      *fc = fu;
+    }
+    return GV_OK;
+  }
+
+  // Brent's minimiser (parabolic interpolation with golden-section
+  // fallback); constants of src/brent.cu:35-37, ITMAX 500.
+  gv_status brent(float ax, float bx, float cx, float tol, float* xmin, float* fret) {
+    const double cgold = 0.3819660, zeps = 1.0e-10;
+    float a = ax < cx ? ax : cx, b = ax > cx ? ax : cx;
+    float d = 0.0f, e = 0.0f, etemp, fu, fv, fw, fx, pp, q, r, tol1, tol2, u, v, w, x, xm;
+    x = w = v = bx;
+    GV_TRY(f1dim(x, &fx));
+    fw = fv = fx;
+    for (int it = 1; it <= 500; it++) {
+      xm = (float)(0.5 * (a + b));
+      tol1 = (float)(tol * std::fabs(x) + zeps);
+      tol2 = (float)(2.0 * tol1);
+      if (std::fabs(x - xm) <= (tol2 - 0.5 * (b - a))) {
+        *xmin = x;
+        *fret = fx;
+        return GV_OK;
+      }
+      if (std::fabs(e) > tol1) {
+        r = (x - w) * (fx - fv);
+        q = (x - v) * (fx - fw);
+        pp = (x - v) * q - (x - w) * r;
+        q = (float)(2.0 * (q - r));
+        if (q > 0.0) pp = -pp;
+        q = std::fabs(q);
+        etemp = e;
+        e = d;
+        if (std::fabs(pp) >= std::fabs(0.5 * q * etemp) || pp <= q * (a - x) ||
+            pp >= q * (b - x)) {
+          e = x >= xm ? a - x : b - x;
+          d = (float)(cgold * e);
+        } else {
+          d = pp / q;
+          u = x + d;
+          if (u - a < tol2 || b - u < tol2) d = signf(tol1, xm - x);
+        }
+      } else {
+        e = x >= xm ? a - x : b - x;
+        d = (float)(cgold * e);
+      }
+      u = std::fabs(d) >= tol1 ? x + d : x + signf(tol1, d);
+      GV_TRY(f1dim(u, &fu));
+      if (fu <= fx) {
+        if (u >= x) a = x; else b = x;
+        v = w; w = x; x = u;
+        fv = fw; fw = fx; fx = fu;
+      } else {
+        if (u < x) a = u; else b = u;
+        if (fu <= fw || w == x) {
+          v = w; w = u; fv = fw; fw = fu;
+        } else if (fu <= fv || v == x || v == w) {
+          v = u; fv = fu;
+        }
+      }
+    }
+    *xmin = x;
+    *fret = fx;
+    return GV_OK;
+  }
+
+  // linmin, src/linmin.cu:52-110
+  gv_status linmin(float* p, float* xi, float* fret) {
+    GV_CUDA(cudaMemcpyAsync(w_.pcom, p, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
+    GV_CUDA(cudaMemcpyAsync(w_.xicom, xi, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
+    float ax = 0.0f, xx = 1.0f, bx, fa, fx, fb, xmin;
+    GV_TRY(bracket(&ax, &xx, &bx, &fa, &fx, &fb));
+    GV_TRY(brent(ax, xx, bx, 1.0e-7f, &xmin, fret));
+    if (verbose()) std::fprintf(stderr, "Alpha for linear minimization = %.9g (f = %.9g)\n", xmin, *fret);
+    k_new_p<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, xmin, floor_val_, floor_cmp_,
+                                                   o_.positivity, p, xi);
+    GV_LAUNCH("k_new_p");
+    return GV_OK;
+  }
+
+  gv_status dot(const float* a, const float* b, int64_t n, double* out) {
+    const int nb = (int)std::min<int64_t>(nblk(n), P_.part_stride);
+    double* part = P_.d_part;
+    k_dot<<<nb, 256, 0, P_.stream>>>(n, a, b, part);
+    k_sum_partials<<<1, 32, 0, P_.stream>>>(nb, part, P_.d_scal + kSlotOpt);
+    GV_LAUNCH("k_dot");
+    GV_TRY(fetch_scalars(P_, kSlotOpt + 1));
+    *out = P_.h_scal[kSlotOpt];
+    return GV_OK;
+  }
+
+  gv_status absmax(const float* x, int64_t n, float* out) {
+    const int nb = (int)std::min<int64_t>(nblk(n), P_.part_stride);
+    k_absmax<<<nb, 256, 0, P_.stream>>>(n, x, P_.d_part);
+    k_max_partials<<<1, 32, 0, P_.stream>>>(nb, P_.d_part, P_.d_scal + kSlotOpt);
+    GV_LAUNCH("k_absmax");
+    GV_TRY(fetch_scalars(P_, kSlotOpt + 1));
+    *out = (float)P_.h_scal[kSlotOpt];
+    return GV_OK;
+  }
+
+  gv_status frprmn(float* img, gv_opt_report* rep) {
+    const int64_t PMN = 2 * MN_;
+    float fp, fret = 0.0f;
+    GV_TRY(func(img, true, &fp));
+    GV_TRY(grad(img, w_.xi, 0));
+    k_cg_init<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, w_.g, w_.xi, w_.h);
+    GV_LAUNCH("k_cg_init");
+    for (int it = 1; it <= o_.total_iterations; it++) {
+      rep->iterations = it;
+      GV_TRY(linmin(img, w_.xi, &fret));
+      if (2.0f * std::fabs(fret - fp) <= o_.ftol * (std::fabs(fret) + std::fabs(fp) + 1.0e-10)) {
+        rep->exit_reason = 1;
+        break;
+      }
+      GV_TRY(func(img, true, &fp));
+      if (verbose()) std::fprintf(stderr, "Iteration %d function value = %.9g\n", it, fp);
+      GV_TRY(grad(img, w_.xi, it));
+      const float den = std::max(fp, 1.0f);
+      const int nb = (int)std::min<int64_t>(nblk(PMN), P_.part_stride);
+      k_cg_stats<<<nb, 256, 0, P_.stream>>>(PMN, den, w_.xi, w_.g, img, P_.d_part,
+                                             P_.part_stride);
+      k_cg_finish<<<1, 32, 0, P_.stream>>>(nb, P_.d_part, P_.part_stride, P_.d_scal + kSlotOpt);
+      GV_LAUNCH("k_cg_stats");
+      GV_TRY(fetch_scalars(P_, kSlotOpt + 3));
+      const float gg = (float)P_.h_scal[kSlotOpt], dgg = (float)P_.h_scal[kSlotOpt + 1];
+      const float gmax = (float)P_.h_scal[kSlotOpt + 2];
+      if (gmax < o_.gtol) {
+        rep->exit_reason = 2;
+        break;
+      }
+      if (gg == 0.0f) {
+        rep->exit_reason = 3;
+        break;
+      }
+      const float gam = std::max(0.0f, dgg / gg);
+      k_new_xi<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, gam, w_.g, w_.xi, w_.h);
+      GV_LAUNCH("k_new_xi");
+    }
+    GV_TRY(func(img, true, &rep->f_final));
+    return GV_OK;
+  }
+
+  gv_status lbfgs(float* img, gv_opt_report* rep) {
+    const int64_t PMN = 2 * MN_;
+    const int K = o_.K;
+    float fp, fret = 0.0f;
+    std::vector<float> alpha(2 * (size_t)K);
+    GV_TRY(func(img, true, &fp));
+    GV_TRY(grad(img, w_.xi, 0));
+    k_scale<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, -1.0f, w_.xi);
+    GV_LAUNCH("k_scale");
+    auto slot = [&](float* base, int im, int k) { return base + MN_ * im * k + MN_ * im; };
+    auto qslot = [&](float* base, int im, int k) { return base + MN_ * im + MN_ * k; };
+    for (int it = 1; it <= o_.total_iterations; it++) {
+      rep->iterations = it;
+      GV_CUDA(cudaMemcpyAsync(w_.p_old, img, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
+      GV_CUDA(cudaMemcpyAsync(w_.xi_old, w_.xi, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
+      GV_TRY(linmin(img, w_.xi, &fret));
+      if ((fp - fret) / std::max({std::fabs(fret), std::fabs(fp), 1.0f}) <= o_.ftol) {
+        rep->exit_reason = 1;
+        break;
+      }
+      float m;
+      GV_TRY(absmax(w_.xi, PMN, &m));
+      const float max_per_it = std::max(0.0f, m);
+      if (max_per_it <= o_.gtol) {
+        rep->exit_reason = 2;
+        break;
+      }
+      GV_TRY(func(img, true, &fp));
+      GV_TRY(grad(img, w_.xi, it));
+      const int lit = (it - 1) % K;
+      for (int im = 0; im < 2; im++) {
+        k_s_and_y<<<nblk(MN_), 256, 0, P_.stream>>>(MN_, w_.xi + MN_ * im, w_.xi_old + MN_ * im,
+                                                    img + MN_ * im, w_.p_old + MN_ * im,
+                                                    slot(d_y_, im, lit), slot(d_s_, im, lit));
+        GV_LAUNCH("k_s_and_y");
+      }
+      // LBFGS_recursion
+      const int par_M = std::min(K, it);
+      GV_CUDA(cudaMemcpyAsync(w_.q, w_.xi, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
+      std::fill(alpha.begin(), alpha.end(), 0.0f);
+      for (int im = 0; im < 2; im++) {
+        for (int k = par_M - 1; k >= 0; k--) {
+          double d1, d2;
+          GV_TRY(dot(slot(d_y_, im, k), slot(d_s_, im, k), MN_, &d1));
+          const float rho_den = (float)d1;
+          const float rho = rho_den != 0.0f ? (float)(1.0 / rho_den) : 0.0f;
+          GV_TRY(dot(slot(d_s_, im, k), w_.q + MN_ * im, MN_, &d2));
+          alpha[im * K + k] = rho * (float)d2;
+          k_axpy<<<nblk(MN_), 256, 0, P_.stream>>>(MN_, -alpha[im * K + k], qslot(d_y_, im, k),
+                                                   w_.q + MN_ * im);
+          GV_LAUNCH("k_axpy");
+        }
+      }
+      float sy_yy = 0.0f;
+      for (int im = 0; im < 2; im++) {
+        double sy, yy;
+        GV_TRY(dot(slot(d_y_, im, lit), slot(d_s_, im, lit), MN_, &sy));
+        GV_TRY(dot(slot(d_y_, im, lit), slot(d_y_, im, lit), MN_, &yy));
+        if ((float)yy != 0.0f) sy_yy += (float)sy / (float)yy;
+      }
+      for (int im = 0; im < 2; im++) {
+        k_scaled_copy<<<nblk(MN_), 256, 0, P_.stream>>>(MN_, sy_yy, w_.q + MN_ * im, w_.r + MN_ * im);
+        GV_LAUNCH("k_scaled_copy");
+        for (int k = 0; k < par_M; k++) {
+          double d1, d2;
+          GV_TRY(dot(slot(d_y_, im, k), slot(d_s_, im, k), MN_, &d1));
+          const float rho_den = (float)d1;
+          const float rho = rho_den != 0.0f ? 1.0f / rho_den : 0.0f;
+          GV_TRY(dot(slot(d_y_, im, k), w_.r + MN_ * im, MN_, &d2));
+          const float beta = rho * (float)d2;
+          k_axpy<<<nblk(MN_), 256, 0, P_.stream>>>(MN_, alpha[im * K + k] - beta,
+                                                   qslot(d_s_, im, k), w_.r + MN_ * im);
+          GV_LAUNCH("k_axpy");
+        }
+      }
+      k_scaled_copy<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, -1.0f, w_.r, w_.xi);
+      GV_LAUNCH("k_scaled_copy");
+    }
+    GV_TRY(func(img, true, &rep->f_final));
+    return GV_OK;
+  }
+
+  int64_t n_obj_ = 0, n_grad_ = 0;
+
+ private:
+  Problem& P_;
+  gv_opt_desc o_;
+  int64_t MN_;
+  float floor_val_;
+  double floor_cmp_;
+  Workspace w_{};
+  float* d_y_ = nullptr;
+  float* d_s_ = nullptr;
+};
+
+}  // namespace
+
+gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep) {
+  if (o.kind != GV_OPT_FRPRMN && o.kind != GV_OPT_LBFGS) {
+    set_error("unknown optimizer kind");
+    return GV_ERR_INVALID;
+  }
+  if (o.total_iterations < 0 || (o.kind == GV_OPT_LBFGS && o.K <= 0)) {
+    set_error("invalid optimizer iterations / memory");
+    return GV_ERR_INVALID;
+  }
+  gv_opt_report r;
+  std::memset(&r, 0, sizeof(r));
+  const auto t0 = std::chrono::steady_clock::now();
+  Solver s(P, o);
+  gv_status st = s.init();
+  if (st == GV_OK) st = o.kind == GV_OPT_FRPRMN ? s.frprmn(d_img, &r) : s.lbfgs(d_img, &r);
+  if (st == GV_OK) {
+    cudaError_t e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "optimize");
+  }
+  r.n_objective = s.n_obj_;
+  r.n_gradient = s.n_grad_;
+  r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rep) *rep = r;
+  return st;
+}
+
+}  // namespace gv

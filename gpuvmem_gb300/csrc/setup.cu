@@ -1,0 +1,487 @@
+// Problem set-up: the per-problem constants the reference prepares in
+// MFS::setDevice (src/mfs.cu:530-943), laid out for GB300.
+//
+//  * calculateNoiseAndBeam (src/functions.cu:1655-1814) on the host, FP64
+//    moments and the FP32 Neumaier weight sum as the reference.
+//  * hermitianSymmetry (src/functions.cu:2256-2273) and the vis_mod cell
+//    choice (src/functions.cu:2557-2609) are evaluated once per visibility
+//    (u,v,w are constant), so weights of visibilities outside the grid are
+//    zeroed here instead of on the first objective evaluation; visibilities
+//    are then sorted by grid cell so the degridding gathers hit L2 in order.
+//  * total_attenuation / weight_image / noise_image, fg_scale = min(noise),
+//    noise_cut = factor * min(noise) (src/mfs.cu:849-916).
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "gv_internal.cuh"
+
+namespace gv {
+
+namespace {
+
+// Neumaier sum in float, src/functions.cu:353-367 (returns the plain sum).
+float neumaier_f(const float* d, int64_t n) {
+  if (n <= 0) return 0.0f;
+  float sum = d[0], c = 0.0f;
+  for (int64_t i = 1; i < n; i++) {
+    float t = sum + d[i];
+    if (std::fabs(sum) >= std::fabs(d[i]))
+      c += (sum - t) + d[i];
+    else
+      c += (d[i] - t) + sum;
+    sum = t;
+  }
+  return sum;
+}
+
+__global__ void k_prepare_vis(int64_t n, int64_t off, int chan, float freq,
+                              const double* __restrict__ uvw_m,
+                              const float2* __restrict__ vo_in,
+                              const float* __restrict__ w_in, double deltau,
+                              double deltav, int N, double dx, double dy,
+                              float4* __restrict__ deg_u,
+                              float2* __restrict__ vo_u, uint4* __restrict__ ph_u,
+                              float* __restrict__ wl_u,
+                              unsigned long long* __restrict__ keys,
+                              int64_t* __restrict__ idx) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t g = off + k;
+  double u = uvw_m[3 * k], v = uvw_m[3 * k + 1], w = uvw_m[3 * k + 2];
+  float2 o = vo_in[k];
+  // hermitianSymmetry
+  if (u > 0.0) {
+    u *= -1.0;
+    v *= -1.0;
+    o.y *= -1.0f;
+  }
+  const float lambda = wavelength(freq);
+  u = u / lambda;
+  v = v / lambda;
+  w = w / lambda;
+  // vis_mod cell choice
+  double ux = u / deltau, uy = v / deltav;
+  if (ux < 0.0) ux += N;
+  if (uy < 0.0) uy += N;
+  const int i1 = __double2int_rd(ux);
+  const int j1 = __double2int_rd(uy);
+  const bool in = (i1 >= 0 && i1 < N && j1 >= 0 && j1 < N);
+  const float wt = in ? w_in[k] : 0.0f;
+  const bool keep = in && wt != 0.0f;
+  const float du = in ? (float)(ux - i1) : 0.0f;
+  const float dv = in ? (float)(uy - j1) : 0.0f;
+  const uint32_t cell = keep ? (uint32_t)j1 * (uint32_t)N + (uint32_t)i1 : 0xFFFFFFFFu;
+  const uint32_t packed = keep ? ((uint32_t)j1 << 16) | (uint32_t)i1 : 0u;
+  deg_u[g] = make_float4(__uint_as_float(packed), du, dv, wt);
+  vo_u[g] = o;
+  // phase constants: exact fixed-point fractions of dx*u and dy*v
+  double tx = dx * u;
+  tx -= floor(tx);
+  double ty = dy * v;
+  ty -= floor(ty);
+  const uint32_t FU = (uint32_t)(unsigned long long)llrint(tx * 4294967296.0);
+  const uint32_t FV = (uint32_t)(unsigned long long)llrint(ty * 4294967296.0);
+  const float GU = (float)(w * dx * dx * 0.5);
+  const float GV = (float)(w * dy * dy * 0.5);
+  ph_u[g] = make_uint4(FU, FV, __float_as_uint(GU), __float_as_uint(GV));
+  wl_u[g] = (float)w;
+  keys[g] = ((unsigned long long)chan << 32) | cell;
+  idx[g] = g;
+}
+
+template <typename T>
+__global__ void k_gather(int64_t n, const int64_t* __restrict__ idx,
+                         const T* __restrict__ in, T* __restrict__ out) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) out[k] = in[idx[k]];
+}
+
+__global__ void k_weight_image(int M, int N, float xobs, float yobs, double DELTAX,
+                               double DELTAY, float nu0, float D, float pbf,
+                               float cut, int pb, float* __restrict__ wimg) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= M) return;
+  const float a = attenuation(i, j, xobs, yobs, DELTAX, DELTAY, nu0, D, pbf, cut, pb);
+  wimg[(int64_t)N * i + j] = a * a;  // weight_image: sum over fields of atten^2
+}
+
+__global__ void k_noise_image(int64_t MN, float max_w, float noise_jypix,
+                              float* __restrict__ img) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= MN) return;
+  const float nsq = noise_jypix * noise_jypix;
+  const float nw = (img[q] / max_w) / nsq;
+  img[q] = sqrtf(1.0f / nw);
+}
+
+__global__ void k_mask(int64_t MN, float cut, const float* __restrict__ noise,
+                       uint8_t* __restrict__ mask) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= MN) return;
+  const float n = noise[q];
+  mask[q] = (n < cut ? kMaskIn : 0) | (n > cut ? kMaskClip : 0);
+}
+
+// rho = (z - 1) + r^2/2 with z = sqrt(1 - r^2), written without
+// cancellation as -r^4 / (2 (1 + z)^2).
+__global__ void k_rho(int M, int N, float xobs, float yobs, double dx, double dy,
+                      float* __restrict__ rho) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= M) return;
+  const int x0 = (int)xobs, y0 = (int)yobs;
+  const double x = (j - x0) * dx, y = (i - y0) * dy;
+  const double r2 = x * x + y * y;
+  const double z = sqrt(1.0 - r2);
+  rho[(int64_t)N * i + j] = (float)(-(r2 * r2) / (2.0 * (1.0 + z) * (1.0 + z)));
+}
+
+}  // namespace
+
+void free_problem(Problem& P) {
+  cudaFree(P.d_deg);
+  cudaFree(P.d_vo);
+  cudaFree(P.d_cvr);
+  cudaFree(P.d_ph);
+  cudaFree(P.d_wl);
+  cudaFree(P.d_perm);
+  cudaFree(P.d_noise);
+  cudaFree(P.d_mask);
+  cudaFree(P.d_rho);
+  cudaFree(P.d_grid);
+  cudaFree(P.d_twiddle);
+  cudaFree(P.d_part);
+  cudaFree(P.d_scal);
+  cudaFree(P.d_tmp);
+  cudaFree(P.d_opt);
+  cudaFree(P.d_lbfgs);
+  cudaFree(P.d_chfreq);
+  cudaFree(P.d_ranges);
+  cudaFree(P.d_chnvis);
+  if (P.h_scal) cudaFreeHost(P.h_scal);
+  P = Problem();
+}
+
+gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
+  // ---- validation (the reference exits on bad input; we return) ----------
+  if (d.M <= 0 || d.N <= 0 || d.M != d.N) {
+    set_error("M and N must be equal and positive (the reference indexes both axes with N)");
+    return GV_ERR_INVALID;
+  }
+  const int n = d.N;
+  if ((n & (n - 1)) != 0 || n < 16 || n > 4096) {
+    set_error("image size must be a power of two between 16 and 4096");
+    return GV_ERR_UNSUPPORTED;
+  }
+  if (d.nchannels <= 0 || d.channels == nullptr) {
+    set_error("at least one channel is required");
+    return GV_ERR_INVALID;
+  }
+  if (d.nterms < 0 || d.nterms > kMaxTerms || (d.nterms > 0 && d.terms == nullptr)) {
+    set_error("between 0 and 8 objective terms are supported");
+    return GV_ERR_INVALID;
+  }
+  if (!(d.deltax_deg != 0.0) || !(d.deltay_deg != 0.0) || !(d.nu_0 > 0.0f)) {
+    set_error("cell sizes must be non-zero and nu_0 positive");
+    return GV_ERR_INVALID;
+  }
+  if (!(d.xobs_pix >= 0.0f && d.xobs_pix < n && d.yobs_pix >= 0.0f && d.yobs_pix < n)) {
+    // src/mfs.cu:692-712 rejects centres outside the image
+    set_error("pointing / phase centre is outside the range of the image");
+    return GV_ERR_INVALID;
+  }
+  P.M = d.M;
+  P.N = d.N;
+  P.log2n = 0;
+  while ((1 << P.log2n) < n) P.log2n++;
+  P.DELTAX = d.deltax_deg;
+  P.DELTAY = d.deltay_deg;
+  P.dx_rad = kRpDegD * d.deltax_deg;
+  P.dy_rad = kRpDegD * d.deltay_deg;
+  P.deltau = 1.0 / (P.M * P.dx_rad);
+  P.deltav = 1.0 / (P.N * P.dy_rad);
+  P.xobs = d.xobs_pix;
+  P.yobs = d.yobs_pix;
+  P.nu_0 = d.nu_0;
+  P.D = d.antenna_diameter;
+  P.pbf = d.pb_factor;
+  P.pbcut = d.pb_cutoff;
+  P.pb = d.primary_beam;
+  P.eta = d.eta;
+  P.minpix = d.initial_value * -1.0f * d.eta;  // src/mfs.cu:167-173
+  P.threshold = d.threshold;
+  P.normalize = d.normalize;
+  // terms: ObjectiveFunction::addFi drops terms whose factor is 0
+  for (int t = 0; t < d.nterms; t++) {
+    const gv_fi_desc& f = d.terms[t];
+    if (f.kind < GV_FI_CHI2 || f.kind > GV_FI_LAPLACIAN) {
+      set_error("unknown objective term kind");
+      return GV_ERR_INVALID;
+    }
+    if (f.image_index < 0 || f.image_index > 1 || f.image_to_add < 0 || f.image_to_add > 1) {
+      set_error("There is no image for the provided index");  // include/classes/fi.cuh:68
+      return GV_ERR_INVALID;
+    }
+    if (f.lambda == 0.0f) continue;
+    if (f.kind == GV_FI_CHI2 && !P.terms.empty()) {
+      set_error("Chi2 must be the first objective term (Chi2::addToDphi overwrites dphi)");
+      return GV_ERR_INVALID;
+    }
+    P.terms.push_back(Term{f.kind, f.lambda, f.image_index, f.image_to_add, f.prior_value,
+                           f.eta, f.epsilon});
+  }
+  int dev = 0;
+  GV_CUDA(cudaGetDevice(&dev));
+  GV_CUDA(cudaDeviceGetAttribute(&P.num_sms, cudaDevAttrMultiProcessorCount, dev));
+
+  // ---- channels ----------------------------------------------------------
+  const int C = d.nchannels;
+  int64_t V = 0;
+  for (int c = 0; c < C; c++) {
+    const gv_channel_desc& ch = d.channels[c];
+    if (ch.nvis < 0 || (ch.nvis > 0 && (!ch.uvw || !ch.vo || !ch.weight)) || !(ch.freq_hz > 0.0f)) {
+      set_error("invalid channel descriptor");
+      return GV_ERR_INVALID;
+    }
+    P.chans.push_back(Channel{ch.freq_hz, ch.nvis, V, 0});
+    V += ch.nvis;
+  }
+  P.V = V;
+  if (V <= 0) {
+    set_error("Max number of visibilities cannot be zero for image synthesis");  // src/mfs.cu:624
+    return GV_ERR_INVALID;
+  }
+
+  // ---- calculateNoiseAndBeam on the host ----------------------------------
+  {
+    float sum_w = 0.0f;
+    double s_uu = 0.0, s_vv = 0.0, s_uv = 0.0;
+    for (int c = 0; c < C; c++) {
+      const gv_channel_desc& ch = d.channels[c];
+      if (ch.nvis <= 0) continue;
+      const float lam = wavelength(ch.freq_hz);
+      double luu = 0.0, lvv = 0.0, luv = 0.0;
+      for (int64_t k = 0; k < ch.nvis; k++) {
+        const double u = ch.uvw[3 * k] / lam, v = ch.uvw[3 * k + 1] / lam;
+        const double w = ch.weight[k];
+        luu += u * u * w;
+        lvv += v * v * w;
+        luv += u * v * w;
+      }
+      s_uu += luu;
+      s_vv += lvv;
+      s_uv += luv;
+      sum_w += neumaier_f(ch.weight, ch.nvis);
+    }
+    if (!(sum_w > 0.0f)) {
+      set_error("The sum of the visibility weights cannot be zero");  // functions.cu:1790
+      return GV_ERR_INVALID;
+    }
+    s_uu /= sum_w;
+    s_vv /= sum_w;
+    s_uv /= sum_w;
+    const float variance = 1.0f / sum_w;
+    const double uu_mv = s_uu - s_vv, uu_pv = s_uu + s_vv;
+    const double sq = std::sqrt(uu_mv * uu_mv + 4.0 * s_uv * s_uv);
+    P.bmaj = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv - sq)) / kRpDegD;
+    P.bmin = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv + sq)) / kRpDegD;
+    P.bpa = (-0.5 * std::atan2(2.0 * s_uv, uu_mv)) / kRpDegD;
+    P.sum_weights = sum_w;
+    P.vis_noise = d.vis_noise > 0.0f ? d.vis_noise : 0.5f * sqrtf(variance);
+  }
+
+  const int64_t MN = (int64_t)P.M * P.N;
+  cudaStream_t st = P.stream;
+
+  // ---- visibilities: upload, prepare, sort by (channel, cell) -------------
+  {
+    double* d_uvw = nullptr;
+    float2* d_vo_in = nullptr;
+    float* d_w_in = nullptr;
+    float4* deg_u = nullptr;
+    float2* vo_u = nullptr;
+    uint4* ph_u = nullptr;
+    float* wl_u = nullptr;
+    unsigned long long *keys = nullptr, *keys2 = nullptr;
+    int64_t *idx = nullptr;
+    void* tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int64_t maxc = 0;
+    for (auto& ch : P.chans) maxc = std::max(maxc, ch.nvis);
+    auto cleanup = [&]() {
+      cudaFree(d_uvw); cudaFree(d_vo_in); cudaFree(d_w_in); cudaFree(deg_u);
+      cudaFree(vo_u); cudaFree(ph_u); cudaFree(wl_u); cudaFree(keys); cudaFree(keys2);
+      cudaFree(idx); cudaFree(tmp);
+    };
+#define GV_SETUP_CUDA(call)                         \
+  do {                                              \
+    cudaError_t _e = (call);                        \
+    if (_e != cudaSuccess) {                        \
+      cleanup();                                    \
+      return cuda_fail(_e, #call);                  \
+    }                                               \
+  } while (0)
+    GV_SETUP_CUDA(cudaMalloc(&d_uvw, sizeof(double) * 3 * std::max<int64_t>(maxc, 1)));
+    GV_SETUP_CUDA(cudaMalloc(&d_vo_in, sizeof(float2) * std::max<int64_t>(maxc, 1)));
+    GV_SETUP_CUDA(cudaMalloc(&d_w_in, sizeof(float) * std::max<int64_t>(maxc, 1)));
+    GV_SETUP_CUDA(cudaMalloc(&deg_u, sizeof(float4) * V));
+    GV_SETUP_CUDA(cudaMalloc(&vo_u, sizeof(float2) * V));
+    GV_SETUP_CUDA(cudaMalloc(&ph_u, sizeof(uint4) * V));
+    GV_SETUP_CUDA(cudaMalloc(&wl_u, sizeof(float) * V));
+    GV_SETUP_CUDA(cudaMalloc(&keys, sizeof(unsigned long long) * V));
+    GV_SETUP_CUDA(cudaMalloc(&keys2, sizeof(unsigned long long) * V));
+    GV_SETUP_CUDA(cudaMalloc(&idx, sizeof(int64_t) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_perm, sizeof(int64_t) * V));
+    for (int c = 0; c < C; c++) {
+      const gv_channel_desc& ch = d.channels[c];
+      if (ch.nvis <= 0) continue;
+      GV_SETUP_CUDA(cudaMemcpyAsync(d_uvw, ch.uvw, sizeof(double) * 3 * ch.nvis,
+                                    cudaMemcpyHostToDevice, st));
+      GV_SETUP_CUDA(cudaMemcpyAsync(d_vo_in, ch.vo, sizeof(float2) * ch.nvis,
+                                    cudaMemcpyHostToDevice, st));
+      GV_SETUP_CUDA(cudaMemcpyAsync(d_w_in, ch.weight, sizeof(float) * ch.nvis,
+                                    cudaMemcpyHostToDevice, st));
+      const int bs = 256;
+      k_prepare_vis<<<(unsigned)((ch.nvis + bs - 1) / bs), bs, 0, st>>>(
+          ch.nvis, P.chans[c].off, c, ch.freq_hz, d_uvw, d_vo_in, d_w_in, P.deltau,
+          P.deltav, P.N, P.dx_rad, P.dy_rad, deg_u, vo_u, ph_u, wl_u, keys, idx);
+      GV_SETUP_CUDA(cudaGetLastError());
+    }
+    GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, idx,
+                                                  P.d_perm, (int64_t)V, 0, 64, st));
+    GV_SETUP_CUDA(cudaMalloc(&tmp, tmp_bytes));
+    GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, idx,
+                                                  P.d_perm, (int64_t)V, 0, 64, st));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_deg, sizeof(float4) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_vo, sizeof(float2) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_ph, sizeof(uint4) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_wl, sizeof(float) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_cvr, sizeof(float2) * V));
+    GV_SETUP_CUDA(cudaMemsetAsync(P.d_cvr, 0, sizeof(float2) * V, st));
+    const unsigned gb = (unsigned)((V + 255) / 256);
+    k_gather<float4><<<gb, 256, 0, st>>>(V, P.d_perm, deg_u, P.d_deg);
+    k_gather<float2><<<gb, 256, 0, st>>>(V, P.d_perm, vo_u, P.d_vo);
+    k_gather<uint4><<<gb, 256, 0, st>>>(V, P.d_perm, ph_u, P.d_ph);
+    k_gather<float><<<gb, 256, 0, st>>>(V, P.d_perm, wl_u, P.d_wl);
+    GV_SETUP_CUDA(cudaGetLastError());
+    // count kept visibilities per channel: keys are sorted, so the kept ones
+    // of channel c are those with key < (c << 32 | 0xFFFFFFFF)
+    std::vector<unsigned long long> hkeys(V);
+    GV_SETUP_CUDA(cudaMemcpyAsync(hkeys.data(), keys2, sizeof(unsigned long long) * V,
+                                  cudaMemcpyDeviceToHost, st));
+    GV_SETUP_CUDA(cudaStreamSynchronize(st));
+    P.Vgrid = 0;
+    for (int c = 0; c < C; c++) {
+      const unsigned long long lim = ((unsigned long long)c << 32) | 0xFFFFFFFFull;
+      auto b = hkeys.begin() + P.chans[c].off;
+      auto e = b + P.chans[c].nvis;
+      P.chans[c].ngrid = std::lower_bound(b, e, lim) - b;
+      P.Vgrid += P.chans[c].ngrid;
+    }
+    // bound of the non-separable w-term residual |w * rho| (cycles)
+    std::vector<float> hw(V);
+    GV_SETUP_CUDA(cudaMemcpy(hw.data(), wl_u, sizeof(float) * V, cudaMemcpyDeviceToHost));
+    double maxw = 0.0;
+    for (float x : hw) maxw = std::max(maxw, (double)std::fabs(x));
+    double rmax = 0.0;
+    {
+      const double hx = std::max(std::fabs((double)(0 - (int)P.xobs)),
+                                 std::fabs((double)(P.M - 1 - (int)P.xobs))) *
+                        std::fabs(P.dx_rad);
+      const double hy = std::max(std::fabs((double)(0 - (int)P.yobs)),
+                                 std::fabs((double)(P.N - 1 - (int)P.yobs))) *
+                        std::fabs(P.dy_rad);
+      const double r2 = hx * hx + hy * hy;
+      const double z = std::sqrt(1.0 - r2);
+      rmax = r2 * r2 / (2.0 * (1.0 + z) * (1.0 + z));
+    }
+    P.max_wrho = maxw * rmax;
+    cleanup();
+#undef GV_SETUP_CUDA
+  }
+
+  // ---- noise image, mask, fg_scale, noise_cut ------------------------------
+  GV_CUDA(cudaMalloc(&P.d_noise, sizeof(float) * MN));
+  GV_CUDA(cudaMalloc(&P.d_mask, MN));
+  GV_CUDA(cudaMalloc(&P.d_rho, sizeof(float) * MN));
+  {
+    dim3 b2(16, 16), g2((P.M + 15) / 16, (P.N + 15) / 16);
+    k_weight_image<<<g2, b2, 0, st>>>(P.M, P.N, P.xobs, P.yobs, P.DELTAX, P.DELTAY, P.nu_0,
+                                      P.D, P.pbf, P.pbcut, P.pb, P.d_noise);
+    GV_LAUNCH("k_weight_image");
+    std::vector<float> h(MN);
+    GV_CUDA(cudaMemcpyAsync(h.data(), P.d_noise, sizeof(float) * MN, cudaMemcpyDeviceToHost, st));
+    GV_CUDA(cudaStreamSynchronize(st));
+    const float max_w = *std::max_element(h.begin(), h.end());
+    const double bmaj_pix = P.bmaj / std::fabs(P.DELTAX);
+    const double bmin_pix = P.bmin / std::fabs(P.DELTAX);
+    const float noise_jypix =
+        (float)(P.vis_noise / (kPiD * bmaj_pix * bmin_pix / (4.0 * logf(2.0f))));
+    k_noise_image<<<(unsigned)((MN + 255) / 256), 256, 0, st>>>(MN, max_w, noise_jypix, P.d_noise);
+    GV_LAUNCH("k_noise_image");
+    GV_CUDA(cudaMemcpyAsync(h.data(), P.d_noise, sizeof(float) * MN, cudaMemcpyDeviceToHost, st));
+    GV_CUDA(cudaStreamSynchronize(st));
+    const float nmin = *std::min_element(h.begin(), h.end());
+    P.fg_scale = nmin;
+    P.noise_cut = d.noise_cut_factor * nmin;
+    int64_t cnt = 0;
+    for (float x : h) cnt += (x < P.noise_cut);
+    P.mask_pixels = cnt;
+    k_mask<<<(unsigned)((MN + 255) / 256), 256, 0, st>>>(MN, P.noise_cut, P.d_noise, P.d_mask);
+    GV_LAUNCH("k_mask");
+    k_rho<<<g2, b2, 0, st>>>(P.M, P.N, P.xobs, P.yobs, P.dx_rad, P.dy_rad, P.d_rho);
+    GV_LAUNCH("k_rho");
+  }
+
+  // ---- FFT twiddles, grids, reduction scratch -----------------------------
+  {
+    std::vector<float2> tw(n / 2);
+    for (int k = 0; k < n / 2; k++) {
+      const double a = 2.0 * kPiD * k / n;
+      tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    GV_CUDA(cudaMalloc(&P.d_twiddle, sizeof(float2) * (n / 2)));
+    GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * (n / 2),
+                            cudaMemcpyHostToDevice, st));
+  }
+  GV_CUDA(cudaMalloc(&P.d_grid, sizeof(float2) * MN * C));
+  {
+    std::vector<float> f(C);
+    std::vector<ChanRange> r(C);
+    std::vector<int64_t> nv(C);
+    for (int c = 0; c < C; c++) {
+      f[c] = P.chans[c].freq;
+      r[c] = ChanRange{P.chans[c].off, P.chans[c].ngrid};
+      nv[c] = P.chans[c].nvis;
+    }
+    GV_CUDA(cudaMalloc(&P.d_chfreq, sizeof(float) * C));
+    GV_CUDA(cudaMalloc(&P.d_ranges, sizeof(ChanRange) * C));
+    GV_CUDA(cudaMalloc(&P.d_chnvis, sizeof(int64_t) * C));
+    GV_CUDA(cudaMemcpy(P.d_chfreq, f.data(), sizeof(float) * C, cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_ranges, r.data(), sizeof(ChanRange) * C, cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_chnvis, nv.data(), sizeof(int64_t) * C, cudaMemcpyHostToDevice));
+  }
+  P.part_stride = 4 * P.num_sms;
+  const int nslots = C + kMaxTerms + 8;
+  GV_CUDA(cudaMalloc(&P.d_part, sizeof(double) * (size_t)P.part_stride * nslots));
+  GV_CUDA(cudaMalloc(&P.d_scal, sizeof(double) * kNumScal));
+  GV_CUDA(cudaMemsetAsync(P.d_scal, 0, sizeof(double) * kNumScal, st));
+  GV_CUDA(cudaMallocHost(&P.h_scal, sizeof(double) * kNumScal));
+  GV_CUDA(cudaMalloc(&P.d_tmp, sizeof(float) * 2 * MN));
+  // DChi2 engine: the tensor-core GEMM needs the w-term to be separable
+  // (|w * rho| below 1e-7 cycles) and a supported geometry.
+  P.engine = d.dchi2_engine;
+  if (P.engine == 0) P.engine = dchi2_tc_supported(P) ? 2 : 1;
+  if (P.engine == 2 && !dchi2_tc_supported(P)) {
+    set_error("tensor-core DChi2 engine not supported for this problem");
+    return GV_ERR_UNSUPPORTED;
+  }
+  GV_CUDA(cudaStreamSynchronize(st));
+  return GV_OK;
+}
+
+}  // namespace gv

@@ -1,0 +1,212 @@
+/*
+ * gpuvmem_gb300 -- C ABI of the GB300-native imaging-objective path.
+ *
+ * The entry points replace the reference's objective/optimiser plugin
+ * surface for one imaging problem (citations are file:line in the gpuvmem
+ * repository):
+ *
+ *   gv_problem_create    MFS::setDevice set-up math (src/mfs.cu:530-943):
+ *                        calculateNoiseAndBeam (src/functions.cu:1700-1814),
+ *                        hermitianSymmetry (src/functions.cu:2256),
+ *                        total_attenuation/weight_image/noise_image and
+ *                        fg_scale/noise_cut (src/mfs.cu:849-916), plus
+ *                        Fi::configure / ObjectiveFunction::addFi wiring
+ *                        (include/classes/fi.cuh:58-89,
+ *                        include/classes/objectivefunction.cuh:9-14)
+ *   gv_chi2              Chi2::calcFi -> chi2() (src/chi2.cu:44-49,
+ *                        src/functions.cu:4323-4454)
+ *   gv_dchi2             Chi2::calcGi -> dchi2() (src/chi2.cu:51-53,
+ *                        src/functions.cu:4456-4558)
+ *   gv_prior_value       Fi::calcFi of Entropy/TSV/TV/L1/Laplacian
+ *                        (src/entropy.cu:42, src/totalsquaredvariation.cu:12,
+ *                        src/totalvariation.cu:26, src/l1norm.cu:26,
+ *                        src/laplacian.cu:12)
+ *   gv_prior_gradient    Fi::calcGi + Fi::addToDphi of the same classes
+ *   gv_objective         ObjectiveFunction::calcFunction
+ *                        (include/classes/objectivefunction.cuh:15-26)
+ *   gv_gradient          ObjectiveFunction::calcGradient
+ *                        (include/classes/objectivefunction.cuh:28-57)
+ *   gv_optimize          Optimizer::optimize of "CG-FRPRMN" and "CG-LBFGS"
+ *                        (src/frprmn.cu:85-195, src/lbfgs.cu:99-341) with
+ *                        linmin/f1dim/mnbrak/brent (src/linmin.cu:52-110,
+ *                        src/f1dim.cu:49-80, src/mnbrak.cu:44-98,
+ *                        src/brent.cu:43-121)
+ *   gv_dirty_image       the DChi2 adjoint applied to the observed data
+ *
+ * Conventions: plain pointers and sizes only.  Image buffers are DEVICE
+ * pointers owned by the caller: 2 planes (I_nu0, alpha) of N rows x M
+ * columns, row-major, plane stride M*N, exactly the reference's layout
+ * (index N*M*plane + N*i + j).  Visibility inputs of gv_problem_create are
+ * HOST pointers.  Every call returns a gv_status; nothing exits the process.
+ * A problem handle is used by one host thread at a time; work is ordered on
+ * the problem's CUDA stream (gv_problem_set_stream).
+ */
+#ifndef GPUVMEM_GB300_H
+#define GPUVMEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gv_status {
+  GV_OK = 0,
+  GV_ERR_INVALID = 1,    /* bad argument or descriptor */
+  GV_ERR_CUDA = 2,       /* a CUDA call failed (see gv_last_error) */
+  GV_ERR_NOMEM = 3,      /* device allocation failed */
+  GV_ERR_UNSUPPORTED = 4,/* size or option not supported by this build */
+  GV_ERR_DEVICE = 5      /* a kernel reported an error status */
+} gv_status;
+
+/* Objective terms, in the order ObjectiveFunction::addFi receives them.
+ * The registration ids of the reference are given for each. */
+typedef enum gv_fi_kind {
+  GV_FI_CHI2 = 0,      /* "Chi2"                  src/chi2.cu:89 */
+  GV_FI_ENTROPY = 1,   /* "Entropy"               src/entropy.cu:75 */
+  GV_FI_TSV = 2,       /* "TotalSquaredVariation" src/totalsquaredvariation.cu:44 */
+  GV_FI_TV = 3,        /* "TotalVariation"        src/totalvariation.cu:60 */
+  GV_FI_L1 = 4,        /* "L1-Norm"               src/l1norm.cu:57 */
+  GV_FI_LAPLACIAN = 5  /* "Laplacian"             src/laplacian.cu:43 */
+} gv_fi_kind;
+
+typedef enum gv_beam { GV_BEAM_AIRYDISK = 0, GV_BEAM_GAUSSIAN = 1 } gv_beam;
+
+typedef struct gv_fi_desc {
+  int32_t kind;         /* gv_fi_kind */
+  float lambda;         /* penalization factor; terms with 0 are dropped
+                           like ObjectiveFunction::addFi */
+  int32_t image_index;  /* plane the prior is evaluated on */
+  int32_t image_to_add; /* plane its gradient is added to */
+  float prior_value;    /* Entropy G (reference default set by main: 0.001) */
+  float eta;            /* Entropy eta (reference default -1) */
+  float epsilon;        /* TV / L1 epsilon (reference default 1e-12) */
+} gv_fi_desc;
+
+/* One spectral channel of one field with one correlation, as the
+ * reference's per-(channel, stokes) visibility arrays (include/MSFITSIO.cuh:90-100). */
+typedef struct gv_channel_desc {
+  float freq_hz;
+  int64_t nvis;
+  const double* uvw;    /* host, 3*nvis: u,v,w in metres (double3 order) */
+  const float* vo;      /* host, 2*nvis: observed visibility re,im */
+  const float* weight;  /* host, nvis: weights after the weighting scheme */
+} gv_channel_desc;
+
+typedef struct gv_problem_desc {
+  int32_t M, N;             /* image columns and rows; M == N, power of two */
+  double deltax_deg;        /* DELTAX (FITS CDELT1, degrees; negative for RA) */
+  double deltay_deg;        /* DELTAY */
+  float xobs_pix, yobs_pix; /* phase / pointing centre in pixels (float) */
+  float nu_0;               /* reference frequency */
+  float antenna_diameter;
+  float pb_factor;
+  float pb_cutoff;
+  int32_t primary_beam;     /* gv_beam */
+  float vis_noise;          /* <= 0: 0.5*sqrt(1/sum w) as the reference */
+  float noise_cut_factor;   /* -N, reference default 10 */
+  float eta;                /* -e, reference default -1 */
+  float initial_value;      /* -z first value; MINPIX = initial_value * -eta */
+  float threshold;          /* 5 * -T, as src/mfs.cu:107 */
+  int32_t normalize;        /* Chi2 normalize flag */
+  int32_t nchannels;
+  const gv_channel_desc* channels;
+  int32_t nterms;
+  const gv_fi_desc* terms;
+  int32_t dchi2_engine;     /* 0 auto, 1 direct SIMT, 2 tensor-core GEMM */
+} gv_problem_desc;
+
+typedef struct gv_problem gv_problem;
+
+typedef struct gv_problem_info {
+  float fg_scale;
+  float noise_cut;       /* absolute */
+  float vis_noise;
+  float minpix;
+  double beam_bmaj_deg, beam_bmin_deg, beam_bpa_deg;
+  float sum_weights;
+  int64_t nvis_total;
+  int64_t nvis_in_grid;  /* visibilities whose weight vis_mod keeps */
+  int64_t mask_pixels;   /* pixels with noise < noise_cut */
+  int32_t dchi2_engine;  /* engine actually used */
+  int32_t nterms;        /* terms kept (lambda != 0) */
+} gv_problem_info;
+
+gv_status gv_problem_create(const gv_problem_desc* desc, gv_problem** out);
+gv_status gv_problem_destroy(gv_problem* p);
+gv_status gv_problem_info_get(const gv_problem* p, gv_problem_info* info);
+/* cudaStream_t passed as void*; NULL = the legacy default stream */
+gv_status gv_problem_set_stream(gv_problem* p, void* stream);
+/* Copies the noise image (M*N floats) to a device buffer. */
+gv_status gv_noise_image(gv_problem* p, float* d_out);
+/* Copies the initial image (plane 0 = MINPIX, plane 1 = 0) to d_img. */
+gv_status gv_initial_image(gv_problem* p, float* d_img);
+
+/* Chi2::calcFi: clips d_img in place (clip2IWNoise), evaluates the model
+ * visibilities, stores the weighted residuals for gv_dchi2 and returns
+ * 0.5*sum w|Vo - Vm|^2 (per-channel /V when normalize). FP64 sum. */
+gv_status gv_chi2(gv_problem* p, float* d_img, int32_t flag_opt, double* chi2);
+/* Chi2::calcGi: d_result (2*M*N, device) += chain-ruled DChi2 of the
+ * residuals stored by the last gv_chi2. */
+gv_status gv_dchi2(gv_problem* p, const float* d_img, int32_t flag_opt,
+                   float* d_result);
+/* Raw DChi2 of one channel (before the chain rule): d_out[M*N] =
+ * -fg*A*sum_k w_k Re(conj(Vr_k) e^{i phi}) (/V when normalize). */
+gv_status gv_dchi2_channel(gv_problem* p, int32_t channel, float* d_out);
+/* Prior value sum (before lambda) of term `term` (index into the kept
+ * terms); evaluated whatever the iteration. */
+gv_status gv_prior_value(gv_problem* p, int32_t term, const float* d_img,
+                         double* value);
+/* d_dphi[plane image_to_add] += lambda * dR/dI of term `term`. */
+gv_status gv_prior_gradient(gv_problem* p, int32_t term, const float* d_img,
+                            float* d_dphi);
+
+/* ObjectiveFunction::calcFunction: sum of lambda*term over the kept terms;
+ * priors contribute only after gv_gradient was called with iter > 0 (the
+ * reference's Fi::iteration).  fi_values (may be NULL) receives each
+ * term's value before lambda. */
+gv_status gv_objective(gv_problem* p, float* d_img, int32_t flag_opt,
+                       double* f, double* fi_values);
+/* ObjectiveFunction::calcGradient into d_xi (2*M*N, device). */
+gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
+                      int32_t flag_opt);
+
+typedef enum gv_optimizer_kind { GV_OPT_FRPRMN = 0, GV_OPT_LBFGS = 1 } gv_optimizer_kind;
+
+typedef struct gv_opt_desc {
+  int32_t kind;             /* gv_optimizer_kind */
+  int32_t total_iterations; /* Optimizer::setTotalIterations */
+  float ftol;               /* Optimizer default 1e-12 */
+  float gtol;               /* Optimizer default 1e-12 */
+  int32_t K;                /* L-BFGS memory, reference default 100 */
+  int32_t flag;             /* Optimizer::setFlag (flag_opt) */
+  int32_t positivity;       /* 1: plane 0 floored at -eta*MINPIX (default) */
+} gv_opt_desc;
+
+typedef struct gv_opt_report {
+  int32_t iterations;
+  int32_t exit_reason;      /* 0 max iterations, 1 ftol, 2 gtol, 3 gg == 0 */
+  float f_final;
+  int64_t n_objective;      /* objective evaluations */
+  int64_t n_gradient;       /* gradient evaluations */
+  double seconds;
+} gv_opt_report;
+
+gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img,
+                      gv_opt_report* report);
+
+/* Dirty image: the DChi2 adjoint applied to w*Vo (no beam, no fg_scale):
+ * d_out[M*N] = sum_c sum_k w Re(conj(Vo) e^{i phi}). */
+gv_status gv_dirty_image(gv_problem* p, float* d_out);
+
+/* Copies the weighted residuals w*(Vo-Vm) of the last gv_chi2, in the
+ * caller's visibility order, to a host buffer of 2*nvis_total floats. */
+gv_status gv_residuals(gv_problem* p, float* h_out);
+
+const char* gv_last_error(void);
+const char* gv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

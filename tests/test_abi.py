@@ -1,0 +1,49 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares
+(no compute calls: this runs without a GPU)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(gv_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ["gv_problem_create", "gv_chi2", "gv_dchi2", "gv_objective", "gv_gradient",
+              "gv_optimize", "gv_last_error"]:
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    import gpuvmem_gb300 as gv
+    if not os.path.exists(gv.LIB_PATH):
+        pytest.fail("libgpuvmem_gb300.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(gv.LIB_PATH)
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(gv.EXPORTS) <= set(declared_symbols())
+
+
+def test_version_and_error_without_gpu():
+    import gpuvmem_gb300 as gv
+    L = gv.lib()
+    assert b"sm_103a" in L.gv_version()
+    # invalid arguments are rejected with a status, never an exit
+    h = ctypes.c_void_p()
+    assert L.gv_problem_create(None, ctypes.byref(h)) == 1
+    assert b"null" in L.gv_last_error()
+    assert L.gv_problem_destroy(None) == 0
