@@ -146,8 +146,7 @@ gv_status gv_dchi2(gv_problem* p, const float* d_img, int32_t flag_opt, float* d
   if (!d_img || !d_result) { gv::set_error("null image or result"); return GV_ERR_INVALID; }
   gv_status s = gv::dchi2_launch(P, d_img, flag_opt, d_result);
   if (s != GV_OK) return s;
-  GV_SYNC(P);
-  return GV_OK;
+  return gv::check_device_error(P);
 }
 
 gv_status gv_dchi2_channel(gv_problem* p, int32_t channel, float* d_out) {
@@ -159,8 +158,7 @@ gv_status gv_dchi2_channel(gv_problem* p, int32_t channel, float* d_out) {
   }
   gv_status s = gv::dchi2_channel_launch(P, channel, d_out);
   if (s != GV_OK) return s;
-  GV_SYNC(P);
-  return GV_OK;
+  return gv::check_device_error(P);
 }
 
 gv_status gv_prior_value(gv_problem* p, int32_t term, const float* d_img, double* value) {
@@ -218,14 +216,15 @@ gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter, in
   if (!d_img || !d_xi || iter < 0) { gv::set_error("invalid gradient arguments"); return GV_ERR_INVALID; }
   gv_status s = gv::gradient_launch(P, d_img, d_xi, iter, flag_opt);
   if (s != GV_OK) return s;
-  GV_SYNC(P);
-  return GV_OK;
+  return gv::check_device_error(P);
 }
 
 gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img, gv_opt_report* report) {
   GV_CHECK_PROBLEM(p);
   if (!opt || !d_img) { gv::set_error("null optimizer descriptor or image"); return GV_ERR_INVALID; }
-  return gv::optimize(p->P, *opt, d_img, report);
+  gv_status s = gv::optimize(p->P, *opt, d_img, report);
+  if (s != GV_OK) return s;
+  return gv::check_device_error(p->P);
 }
 
 gv_status gv_dirty_image(gv_problem* p, float* d_out) {
@@ -234,8 +233,7 @@ gv_status gv_dirty_image(gv_problem* p, float* d_out) {
   if (!d_out) { gv::set_error("null output"); return GV_ERR_INVALID; }
   gv_status s = gv::dirty_launch(P, d_out);
   if (s != GV_OK) return s;
-  GV_SYNC(P);
-  return GV_OK;
+  return gv::check_device_error(P);
 }
 
 gv_status gv_residuals(gv_problem* p, float* h_out) {

@@ -1,15 +1,621 @@
-// Tensor-core DChi2 engine (tcgen05); see dchi2_direct.cu for the exact
-// SIMT engine used when this one does not apply.
+// DChi2 on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// The reference's direct sum (src/functions.cu:3698-3791)
+//   S(i,j) = sum_k w_k Re(conj(Vr_k) e^{2 pi i theta_k(i,j)}),
+//   theta_k(i,j) = x_j u_k + y_i v_k + (z_ij - 1) w_k,
+// is a complex GEMM once the phase is split into per-row and per-column
+// factors: with (z-1) = -(x^2+y^2)/2 + rho and |w rho| below 1e-7 cycles
+// (checked at set-up),
+//   e^{2 pi i theta} = b_k(i) a_k(j),  b_k(i) = e^{2 pi i (y_i v_k - w_k y_i^2/2)},
+//                                     a_k(j) = e^{2 pi i (x_j u_k - w_k x_j^2/2)},
+//   S(i,j) = Re sum_k b_k(i) x_k(j),  x_k(j) = conj(w_k Vr_k) a_k(j),
+// i.e. a real GEMM D = A B with K = 2V:  A[i][2k] = Re b, A[i][2k+1] = Im b,
+// B[2k][j] = Re x, B[2k+1][j] = -Im x.
+//
+// Operands are never materialised in HBM.  Per chunk of 32 visibilities the
+// CTA's 8 warps generate the 128 x 64 A tile and the TN x 64 B tile in
+// shared memory: each thread produces 8 consecutive rows for one
+// visibility from an exact fixed-point anchor (the linear phase is reduced
+// mod 1 with 32-bit integer products) and a chirp recurrence in FP32.  Each
+// operand is split into FP16 hi + lo parts and the tile is accumulated with
+// three MMAs (hi*hi + hi*lo + lo*hi) into an FP32 accumulator in TMEM.
+// Operand tiles are MN-major with the 128-byte swizzle; two stages let the
+// tensor core work on chunk n while the warps generate chunk n+1.  Every
+// 16 chunks the accumulator is drained into a running sum held in the other
+// half of TMEM (short FP32 accumulation chains); at the end of each channel
+// the running sum is multiplied by the channel's epilogue factor (beam,
+// fg_scale, chain rule) and added to this split's partial image.  Split-K
+// partials are summed in FP64 in a fixed order, so results are
+// deterministic.
+//
+// Every wait on an mbarrier is bounded: on timeout the kernel records an
+// error word, stops issuing work, waits (bounded) for its own MMAs, frees
+// its TMEM and returns; the host turns the word into GV_ERR_DEVICE.
+#include <cuda_fp16.h>
+
+#include <cstdint>
+
 #include "gv_internal.cuh"
 
 namespace gv {
 
-bool dchi2_tc_supported(const Problem& P) { return false; }
+namespace tc {
+
+constexpr int kTM = 128;          // image rows per tile (MMA M)
+constexpr int kChunkVis = 32;     // visibilities per chunk
+constexpr int kKC = 2 * kChunkVis;  // K elements per chunk
+constexpr int kThreads = 256;
+constexpr int kSlab = 16;         // chunks accumulated before a drain
+constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+struct VisEntry {
+  uint32_t FU, FV;
+  float GU, GV;
+  float2 Eu, Ev;
+  float2 c;  // conj(w Vr) * scale
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// ---- tcgen05 / mbarrier wrappers (inline PTX) -------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(m, parity)) {
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(slot)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(mbar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+      "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+      "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+      "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+      "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+      "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+      "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+      "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading byte
+// offset (stride between 64-element MN atoms for MN-major swizzled layouts),
+// stride byte offset (stride between 8-row K atoms), version 1, 128-byte
+// swizzle.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = F16, both MN-major.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | (1u << 15) | (1u << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of element (row m, k-index kk) in an MN-major 128B-swizzled
+// tile whose MN atoms (64 rows) are 1024 B apart and K atoms (8 rows) are
+// sbo apart; the 16-byte chunk holds rows 8*oct .. 8*oct+7.
+__device__ __forceinline__ uint32_t tile_off(int matom, int oct, int kk, uint32_t sbo) {
+  const int katom = kk >> 3, krow = kk & 7;
+  return (uint32_t)(katom * sbo + matom * 1024 + krow * 128 + ((oct ^ krow) << 4));
+}
+
+struct TcParams {
+  int N;           // image is N x N
+  int64_t MN;
+  int x0, y0;      // int-truncated centre (DChi2 coordinates)
+  float xobs, yobs, nu_0, D, pbf, pbcut, fg_scale, threshold;
+  int pb;
+  double DELTAX, DELTAY;
+  int normalize, flag_opt, mode;
+  int ntile_i, ntile_j, nsplit;
+  int C;
+  int64_t Ktot;                  // kept visibilities over all channels
+  const int64_t* kc_off;         // [C+1] compact offsets of kept visibilities
+  const ChanRange* ranges;       // [C]
+  const float* chfreq;
+  const int64_t* chnvis;
+  const uint4* ph;
+  const float4* E;
+  const float2* cvr;
+  const float4* deg;
+  const float2* vo;
+  const uint8_t* mask;
+  const float* img;
+  const uint32_t* cmax_bits;     // max |c| (float bits)
+  float* partial;                // [nsplit][MN]
+  uint32_t* err;
+};
+
+template <int TN>
+struct Layout {
+  static constexpr uint32_t kSboA = (kTM / 64) * 1024;   // bytes between K atoms of A
+  static constexpr uint32_t kSboB = (TN / 64) * 1024;
+  static constexpr uint32_t kTileA = kSboA * (kKC / 8);  // one A part (hi or lo)
+  static constexpr uint32_t kTileB = kSboB * (kKC / 8);
+  static constexpr uint32_t kStage = 2 * kTileA + 2 * kTileB;
+  static constexpr uint32_t kVis = 2 * kChunkVis * sizeof(VisEntry);
+  static constexpr uint32_t kSmem = 1024 + 2 * kStage + kVis + 64;
+};
+
+// Epilogue factor of one pixel for channel c (mode 0: gradient with chain
+// rule; 1: raw channel DChi2; 2: dirty image), divided by the operand scale.
+__device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int j, float inv_s) {
+  if (p.mode == 2) return inv_s;
+  const int64_t q = (int64_t)p.N * i + j;
+  if (!(p.mask[q] & kMaskIn)) return 0.0f;
+  const float freq = p.chfreq[c];
+  const float atten = attenuation(i, j, p.xobs, p.yobs, p.DELTAX, p.DELTAY, freq, p.D, p.pbf,
+                                  p.pbcut, p.pb);
+  float f = -(p.fg_scale * atten) * inv_s;
+  if (p.normalize) f /= (float)p.chnvis[c];
+  if (p.mode == 1) return f;
+  const float nudiv = freq / p.nu_0;
+  const float i0 = p.img[q], al = p.img[p.MN + q];
+  const float pw = powf(nudiv, al);
+  if (p.flag_opt % 2 == 0) return f * pw;
+  if (i0 > p.threshold) return f * (i0 * pw * p.fg_scale * logf(nudiv));
+  return 0.0f;
+}
+
+// Generate 8 consecutive rows of one operand for one visibility and store
+// the FP16 hi/lo parts of Re and (sign-adjusted) Im.
+template <bool kIsB>
+__device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* hi, uint8_t* lo,
+                                          int matom, int oct, int kv, uint32_t sbo) {
+  const uint32_t F = kIsB ? ve.FU : ve.FV;
+  const float G = kIsB ? ve.GU : ve.GV;
+  const float2 E = kIsB ? ve.Eu : ve.Ev;
+  const float rf = (float)r0;
+  const uint32_t lin = (uint32_t)r0 * F;
+  float th = (float)(int32_t)lin * 2.3283064365386963e-10f;
+  th = fmaf(-rf * rf, G, th);
+  float sn, cs;
+  sincospif(2.0f * th, &sn, &cs);
+  float2 v = make_float2(cs, sn);
+  if (kIsB) v = cmul(v, ve.c);
+  const float eps = -6.283185307179586f * G * (2.0f * rf + 1.0f);
+  float2 d = cmul(E, make_float2(1.0f - 0.5f * eps * eps, eps));
+  const float eq = -12.566370614359172f * G;
+  const float2 q = make_float2(1.0f - 0.5f * eq * eq, eq);
+  float re[8], im[8];
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    re[t] = v.x;
+    im[t] = kIsB ? -v.y : v.y;
+    if (t < 7) {
+      v = cmul(v, d);
+      d = cmul(d, q);
+    }
+  }
+  uint32_t hre[4], him[4], lre[4], lim[4];
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const __half2 h_re = __floats2half2_rn(re[2 * t], re[2 * t + 1]);
+    const __half2 h_im = __floats2half2_rn(im[2 * t], im[2 * t + 1]);
+    const float2 b_re = __half22float2(h_re);
+    const float2 b_im = __half22float2(h_im);
+    const __half2 l_re = __floats2half2_rn(re[2 * t] - b_re.x, re[2 * t + 1] - b_re.y);
+    const __half2 l_im = __floats2half2_rn(im[2 * t] - b_im.x, im[2 * t + 1] - b_im.y);
+    hre[t] = *reinterpret_cast<const uint32_t*>(&h_re);
+    him[t] = *reinterpret_cast<const uint32_t*>(&h_im);
+    lre[t] = *reinterpret_cast<const uint32_t*>(&l_re);
+    lim[t] = *reinterpret_cast<const uint32_t*>(&l_im);
+  }
+  const uint32_t ore = tile_off(matom, oct, 2 * kv, sbo);
+  const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, sbo);
+  *reinterpret_cast<uint4*>(hi + ore) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+  *reinterpret_cast<uint4*>(hi + oim) = make_uint4(him[0], him[1], him[2], him[3]);
+  *reinterpret_cast<uint4*>(lo + ore) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+  *reinterpret_cast<uint4*>(lo + oim) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
+}
+
+template <int TN>
+__global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
+  using L = Layout<TN>;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint8_t* stage_ptr[2] = {base, base + L::kStage};
+  VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + 2 * L::kStage);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tmem_alloc(tslot, kTmemCols);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t t_acc = tbase;
+  const uint32_t t_run = tbase + 256;
+
+  // operand scale: c * 2^-e with max |c| * 2^-e <= 1
+  const float cmax = __uint_as_float(*p.cmax_bits);
+  int e = 0;
+  if (cmax > 0.0f) frexpf(cmax, &e);
+  const float scale = ldexpf(1.0f, -e);
+  const float inv_s = ldexpf(1.0f, e);
+  const uint32_t idesc = make_idesc(kTM, TN);
+
+  // drain / epilogue geometry: warp -> 32 TMEM lanes and a column half
+  const int lq = warp & 3, half = warp >> 2;
+  constexpr int kColsPerThread = TN / 2;
+  const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
+
+  uint32_t nch = 0;  // chunks issued by this CTA (stage = nch & 1)
+  bool ok = true;
+  const int nitems = p.ntile_i * p.ntile_j * p.nsplit;
+  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    const int split = item % p.nsplit;
+    const int tile = item / p.nsplit;
+    const int ti = tile / p.ntile_j, tj = tile % p.ntile_j;
+    const int i0 = ti * kTM, j0 = tj * TN;
+    const int64_t ks = p.Ktot * split / p.nsplit, ke = p.Ktot * (split + 1) / p.nsplit;
+    bool first_channel = true;
+    // this thread's epilogue pixels
+    const int ei = i0 + 32 * lq + lane;
+    const int ej0 = j0 + half * kColsPerThread;
+    float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + ej0;
+    for (int c = 0; c < p.C && ok; c++) {
+      const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
+      const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
+      if (a >= b) continue;
+      const int64_t goff = p.ranges[c].off + (a - cs);
+      const int64_t nvis = b - a;
+      const int nchunks = (int)((nvis + kChunkVis - 1) / kChunkVis);
+      bool run_empty = true;
+      for (int n = 0; n < nchunks && ok; n++) {
+        const int st = nch & 1;
+        uint8_t* sp = stage_ptr[st];
+        if (nch >= 2) {
+          if (!mbar_wait(&mbar[st], ((nch >> 1) - 1) & 1)) {
+            atomicExch(p.err, 1u);
+            s_abort = 1;
+          }
+        }
+        __syncthreads();
+        if (s_abort) {
+          ok = false;
+          break;
+        }
+        // stage the chunk's per-visibility constants
+        if (tid < kChunkVis) {
+          VisEntry ve;
+          const int64_t kidx = (int64_t)n * kChunkVis + tid;
+          if (kidx < nvis) {
+            const int64_t g = goff + kidx;
+            const uint4 ph = p.ph[g];
+            const float4 E = p.E[g];
+            float2 cc;
+            if (p.mode == 2) {
+              const float4 d = p.deg[g];
+              const float2 o = p.vo[g];
+              cc = make_float2(d.w * o.x, -(d.w * o.y));
+            } else {
+              const float2 r = p.cvr[g];
+              cc = make_float2(r.x, -r.y);
+            }
+            ve.FU = ph.x;
+            ve.FV = ph.y;
+            ve.GU = __uint_as_float(ph.z);
+            ve.GV = __uint_as_float(ph.w);
+            ve.Eu = make_float2(E.x, E.y);
+            ve.Ev = make_float2(E.z, E.w);
+            ve.c = make_float2(cc.x * scale, cc.y * scale);
+          } else {
+            ve.FU = ve.FV = 0u;
+            ve.GU = ve.GV = 0.0f;
+            ve.Eu = ve.Ev = make_float2(1.0f, 0.0f);
+            ve.c = make_float2(0.0f, 0.0f);
+          }
+          s_vis[st * kChunkVis + tid] = ve;
+        }
+        __syncthreads();
+        // generate: A (image rows) 2 atoms x 8 visibility quads, then B
+        uint8_t* a_hi = sp;
+        uint8_t* a_lo = sp + L::kTileA;
+        uint8_t* b_hi = sp + 2 * L::kTileA;
+        uint8_t* b_lo = sp + 2 * L::kTileA + L::kTileB;
+        const int oct = lane & 7, kq = lane >> 3;
+        constexpr int kTasksA = (kTM / 64) * (kChunkVis / 4);
+        constexpr int kTasksB = (TN / 64) * (kChunkVis / 4);
+        for (int wt = warp; wt < kTasksA + kTasksB; wt += kThreads / 32) {
+          if (wt < kTasksA) {
+            const int matom = wt / (kChunkVis / 4);
+            const int kv = (wt % (kChunkVis / 4)) * 4 + kq;
+            const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
+            gen_octet<false>(s_vis[st * kChunkVis + kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA);
+          } else {
+            const int w2 = wt - kTasksA;
+            const int matom = w2 / (kChunkVis / 4);
+            const int kv = (w2 % (kChunkVis / 4)) * 4 + kq;
+            const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
+            gen_octet<true>(s_vis[st * kChunkVis + kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB);
+          }
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+          fence_after();
+          const uint32_t sa_hi = smem_u32(a_hi), sa_lo = smem_u32(a_lo);
+          const uint32_t sb_hi = smem_u32(b_hi), sb_lo = smem_u32(b_lo);
+          const bool fresh = (n % kSlab) == 0;
+#pragma unroll
+          for (int t = 0; t < kKC / 16; t++) {
+            const uint64_t ah = make_desc(sa_hi + t * 2 * L::kSboA, 1024, L::kSboA);
+            const uint64_t al = make_desc(sa_lo + t * 2 * L::kSboA, 1024, L::kSboA);
+            const uint64_t bh = make_desc(sb_hi + t * 2 * L::kSboB, 1024, L::kSboB);
+            const uint64_t bl = make_desc(sb_lo + t * 2 * L::kSboB, 1024, L::kSboB);
+            mma_f16(t_acc, ah, bh, idesc, (fresh && t == 0) ? 0u : 1u);
+            mma_f16(t_acc, ah, bl, idesc, 1u);
+            mma_f16(t_acc, al, bh, idesc, 1u);
+          }
+          mma_commit(&mbar[st]);
+        }
+        const bool last = (n == nchunks - 1);
+        const bool drain = last || ((n % kSlab) == kSlab - 1);
+        const uint32_t my_commit = nch >> 1;
+        nch++;
+        if (drain) {
+          if (!mbar_wait(&mbar[st], my_commit & 1)) {
+            atomicExch(p.err, 2u);
+            s_abort = 1;
+          }
+          __syncthreads();
+          if (s_abort) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          // running sum += accumulator (short FP32 chains)
+#pragma unroll 1
+          for (int cb = 0; cb < kColsPerThread; cb += 32) {
+            const uint32_t col = (uint32_t)(half * kColsPerThread + cb);
+            float acc[32], run[32];
+            tmem_ld32(t_acc + lane_off + col, acc);
+            if (!run_empty) {
+              tmem_ld32(t_run + lane_off + col, run);
+#pragma unroll
+              for (int k = 0; k < 32; k++) acc[k] += run[k];
+            }
+            tmem_st32(t_run + lane_off + col, acc);
+          }
+          run_empty = false;
+          if (last) {
+            // channel epilogue: partial (+)= factor * running sum
+#pragma unroll 1
+            for (int cb = 0; cb < kColsPerThread; cb += 32) {
+              const uint32_t col = (uint32_t)(half * kColsPerThread + cb);
+              float run[32];
+              tmem_ld32(t_run + lane_off + col, run);
+#pragma unroll 4
+              for (int k = 0; k < 32; k++) {
+                const float f = epi_factor(p, c, ei, ej0 + cb + k, inv_s);
+                const float v = f * run[k];
+                if (first_channel)
+                  prow[cb + k] = v;
+                else
+                  prow[cb + k] += v;
+              }
+            }
+            first_channel = false;
+          }
+          fence_before();
+          __syncthreads();
+        }
+      }
+    }
+    if (ok && first_channel) {
+      // no visibilities in this split for this tile: its partial is zero
+      for (int k = 0; k < kColsPerThread; k++) prow[k] = 0.0f;
+    }
+  }
+  // retire: make sure no MMA is still reading shared memory / writing TMEM
+  if (nch > 0) {
+    const uint32_t st = (nch - 1) & 1;
+    const uint32_t last_commit = (nch - 1) >> 1;
+    if (!mbar_wait(&mbar[st], last_commit & 1)) atomicExch(p.err, 3u);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0) tmem_dealloc(tbase, kTmemCols);
+}
+
+// result[plane][q] += sum_s partial[s][q] (FP64, fixed order)
+__global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restrict__ partial,
+                                  float* __restrict__ out) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= MN) return;
+  double s = 0.0;
+  for (int k = 0; k < nsplit; k++) s += (double)partial[(int64_t)k * MN + q];
+  out[q] += (float)s;
+}
+
+}  // namespace tc
+
+bool dchi2_tc_supported(const Problem& P) {
+  return P.N >= 128 && P.N == P.M && P.max_wrho < 1e-7 && P.tc_partial != nullptr;
+}
+
+int tc_tile_n(const Problem& P) { return P.N >= 256 ? 256 : 128; }
+
+size_t tc_smem_bytes(int tn) {
+  return tn == 256 ? tc::Layout<256>::kSmem : tc::Layout<128>::kSmem;
+}
 
 gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result,
                    int only_channel, int mode) {
-  set_error("tensor-core DChi2 engine not available");
-  return GV_ERR_UNSUPPORTED;
+  if (!dchi2_tc_supported(P)) {
+    set_error("tensor-core DChi2 engine not supported for this problem");
+    return GV_ERR_UNSUPPORTED;
+  }
+  tc::TcParams p;
+  p.N = P.N;
+  p.MN = (int64_t)P.M * P.N;
+  p.x0 = (int)P.xobs;
+  p.y0 = (int)P.yobs;
+  p.xobs = P.xobs;
+  p.yobs = P.yobs;
+  p.nu_0 = P.nu_0;
+  p.D = P.D;
+  p.pbf = P.pbf;
+  p.pbcut = P.pbcut;
+  p.fg_scale = P.fg_scale;
+  p.threshold = P.threshold;
+  p.pb = P.pb;
+  p.DELTAX = P.DELTAX;
+  p.DELTAY = P.DELTAY;
+  p.normalize = P.normalize;
+  p.flag_opt = flag_opt;
+  p.mode = mode;
+  const int TN = tc_tile_n(P);
+  p.ntile_i = P.N / tc::kTM;
+  p.ntile_j = P.N / TN;
+  p.nsplit = P.tc_nsplit;
+  p.ranges = P.d_ranges;
+  p.chfreq = P.d_chfreq;
+  p.chnvis = P.d_chnvis;
+  p.ph = P.d_ph;
+  p.E = P.d_E;
+  p.cvr = P.d_cvr;
+  p.deg = P.d_deg;
+  p.vo = P.d_vo;
+  p.mask = P.d_mask;
+  p.img = d_img;
+  p.partial = P.tc_partial;
+  p.err = P.d_flags + kFlagErr;
+  p.cmax_bits = P.d_flags + (mode == 2 ? kFlagDirtyMax : kFlagCvrMax);
+  if (only_channel >= 0) {
+    p.C = 1;
+    p.kc_off = P.d_kc_one + 2 * only_channel;
+    p.ranges = P.d_ranges + only_channel;
+    p.chfreq = P.d_chfreq + only_channel;
+    p.chnvis = P.d_chnvis + only_channel;
+    p.Ktot = P.chans[only_channel].ngrid;
+  } else {
+    p.C = (int)P.chans.size();
+    p.kc_off = P.d_kc_off;
+    p.Ktot = P.Vgrid;
+  }
+  const int nitems = p.ntile_i * p.ntile_j * p.nsplit;
+  const int grid = nitems < P.num_sms ? nitems : P.num_sms;
+  const size_t smem = tc_smem_bytes(TN);
+  if (TN == 256) {
+    GV_CUDA(cudaFuncSetAttribute(tc::k_dchi2_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    tc::k_dchi2_tc<256><<<grid, tc::kThreads, smem, P.stream>>>(p);
+  } else {
+    GV_CUDA(cudaFuncSetAttribute(tc::k_dchi2_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    tc::k_dchi2_tc<128><<<grid, tc::kThreads, smem, P.stream>>>(p);
+  }
+  GV_LAUNCH("k_dchi2_tc");
+  float* out = d_result + (mode == 0 ? (int64_t)(flag_opt % 2) * p.MN : 0);
+  tc::k_reduce_partials<<<(unsigned)((p.MN + 255) / 256), 256, 0, P.stream>>>(
+      p.MN, p.nsplit, P.tc_partial, out);
+  GV_LAUNCH("k_reduce_partials");
+  return GV_OK;
 }
 
 }  // namespace gv

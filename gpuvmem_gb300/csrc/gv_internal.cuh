@@ -35,6 +35,14 @@ enum ScalarSlot {
 };
 constexpr int kMaxTerms = 8;
 
+// Word slots in Problem::d_flags (uint32, device).
+enum FlagSlot {
+  kFlagCvrMax = 0,    // max |w Vr| component of the last stored residuals (float bits)
+  kFlagDirtyMax = 1,  // max |w Vo| component (float bits)
+  kFlagErr = 2,       // non-zero: a kernel gave up on a bounded wait
+  kNumFlags = 8
+};
+
 struct Channel {
   float freq;
   int64_t nvis;   // visibilities of this channel (all, incl. zero weight)
@@ -107,6 +115,12 @@ struct Problem {
   float* d_chfreq = nullptr;     // [C] channel frequencies
   ChanRange* d_ranges = nullptr; // [C] kept-visibility ranges
   int64_t* d_chnvis = nullptr;   // [C] visibilities per channel (normalize)
+  int64_t* d_kc_off = nullptr;   // [C+1] offsets of kept visibilities, channels concatenated
+  int64_t* d_kc_one = nullptr;   // [2C] {0, ngrid_c} per channel
+  float4* d_E = nullptr;         // [V] {e^{2 pi i FU/2^32}, e^{2 pi i FV/2^32}}
+  uint32_t* d_flags = nullptr;   // [kNumFlags]
+  float* tc_partial = nullptr;   // [tc_nsplit][MN] split-K partial images
+  int tc_nsplit = 0;
   int num_sms = 0;
 };
 
@@ -179,6 +193,8 @@ gv_status dchi2_direct(Problem& P, const float* d_img, int flag_opt, float* d_re
 gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result,
                    int only_channel, int mode);
 bool dchi2_tc_supported(const Problem& P);
+int tc_tile_n(const Problem& P);
+gv_status check_device_error(Problem& P);
 
 // optimiser
 gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep);

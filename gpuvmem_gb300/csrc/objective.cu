@@ -170,8 +170,9 @@ __global__ void __launch_bounds__(256) k_degrid(
     int N, int64_t MN, const ChanRange* __restrict__ ranges,
     const float4* __restrict__ deg, const float2* __restrict__ vo,
     const float2* __restrict__ grid, float2* __restrict__ cvr, int store,
-    double* __restrict__ part, int part_stride) {
+    double* __restrict__ part, int part_stride, uint32_t* __restrict__ cmax) {
   const int c = blockIdx.y;
+  float mx = 0.0f;
   const ChanRange rg = ranges[c];
   const float2* __restrict__ G = grid + (int64_t)c * MN;
   const int nm1 = N - 1;
@@ -194,7 +195,15 @@ __global__ void __launch_bounds__(256) k_degrid(
     const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
     const float rr = o.x - mr, ri = o.y - mi;
     acc += (double)(d.w * (rr * rr + ri * ri));
-    if (store) __stcs(cvr + rg.off + k, make_float2(d.w * rr, d.w * ri));
+    if (store) {
+      const float2 cv = make_float2(d.w * rr, d.w * ri);
+      __stcs(cvr + rg.off + k, cv);
+      mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
+    }
+  }
+  if (store) {
+    for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, s));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(cmax, __float_as_uint(mx));
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = acc;
@@ -396,8 +405,10 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
   int nb = (int)std::min<int64_t>((maxg + 255) / 256, P.part_stride);
   if (nb < 1) nb = 1;
   const int64_t MN = (int64_t)P.M * P.N;
+  if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
   k_degrid<<<dim3(nb, C), 256, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
-                                              P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride);
+                                              P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride,
+                                              P.d_flags + kFlagCvrMax);
   GV_LAUNCH("k_degrid");
   k_finish_chi2<<<1, 256, 0, P.stream>>>(C, nb, P.d_part, P.part_stride, P.d_chnvis, P.normalize,
                                          P.d_scal + kSlotChi2);
@@ -461,6 +472,19 @@ gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_re
       GV_CUDA(cudaMemsetAsync(P.d_scal + kSlotTerm0 + t, 0, sizeof(double), P.stream));
     }
     if (s != GV_OK) return s;
+  }
+  return GV_OK;
+}
+
+gv_status check_device_error(Problem& P) {
+  uint32_t e = 0;
+  GV_CUDA(cudaMemcpyAsync(&e, P.d_flags + kFlagErr, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                          P.stream));
+  GV_CUDA(cudaStreamSynchronize(P.stream));
+  if (e != 0) {
+    GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagErr, 0, sizeof(uint32_t), P.stream));
+    set_error("a kernel gave up on a bounded wait (device error word " + std::to_string(e) + ")");
+    return GV_ERR_DEVICE;
   }
   return GV_OK;
 }

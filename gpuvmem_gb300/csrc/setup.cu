@@ -44,7 +44,7 @@ __global__ void k_prepare_vis(int64_t n, int64_t off, int chan, float freq,
                               double deltav, int N, double dx, double dy,
                               float4* __restrict__ deg_u,
                               float2* __restrict__ vo_u, uint4* __restrict__ ph_u,
-                              float* __restrict__ wl_u,
+                              float* __restrict__ wl_u, float4* __restrict__ E_u,
                               unsigned long long* __restrict__ keys,
                               int64_t* __restrict__ idx) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -87,6 +87,11 @@ __global__ void k_prepare_vis(int64_t n, int64_t off, int chan, float freq,
   const float GU = (float)(w * dx * dx * 0.5);
   const float GV = (float)(w * dy * dy * 0.5);
   ph_u[g] = make_uint4(FU, FV, __float_as_uint(GU), __float_as_uint(GV));
+  // unit phasors of the fixed-point fractions (exact angle, FP64 sincos)
+  double su, cu, sv, cv;
+  sincospi(2.0 * (double)(int32_t)FU * 2.3283064365386963e-10, &su, &cu);
+  sincospi(2.0 * (double)(int32_t)FV * 2.3283064365386963e-10, &sv, &cv);
+  E_u[g] = make_float4((float)cu, (float)su, (float)cv, (float)sv);
   wl_u[g] = (float)w;
   keys[g] = ((unsigned long long)chan << 32) | cell;
   idx[g] = g;
@@ -97,6 +102,19 @@ __global__ void k_gather(int64_t n, const int64_t* __restrict__ idx,
                          const T* __restrict__ in, T* __restrict__ out) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k < n) out[k] = in[idx[k]];
+}
+
+__global__ void k_dirty_max(int64_t V, const float4* __restrict__ deg,
+                            const float2* __restrict__ vo, uint32_t* __restrict__ out) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (k < V) {
+    const float4 d = deg[k];
+    const float2 o = vo[k];
+    m = fmaxf(fabsf(d.w * o.x), fabsf(d.w * o.y));
+  }
+  for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, s));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(out, __float_as_uint(m));
 }
 
 __global__ void k_weight_image(int M, int N, float xobs, float yobs, double DELTAX,
@@ -162,6 +180,11 @@ void free_problem(Problem& P) {
   cudaFree(P.d_chfreq);
   cudaFree(P.d_ranges);
   cudaFree(P.d_chnvis);
+  cudaFree(P.d_kc_off);
+  cudaFree(P.d_kc_one);
+  cudaFree(P.d_E);
+  cudaFree(P.d_flags);
+  cudaFree(P.tc_partial);
   if (P.h_scal) cudaFreeHost(P.h_scal);
   P = Problem();
 }
@@ -306,6 +329,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     float2* vo_u = nullptr;
     uint4* ph_u = nullptr;
     float* wl_u = nullptr;
+    float4* E_u = nullptr;
     unsigned long long *keys = nullptr, *keys2 = nullptr;
     int64_t *idx = nullptr;
     void* tmp = nullptr;
@@ -314,7 +338,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     for (auto& ch : P.chans) maxc = std::max(maxc, ch.nvis);
     auto cleanup = [&]() {
       cudaFree(d_uvw); cudaFree(d_vo_in); cudaFree(d_w_in); cudaFree(deg_u);
-      cudaFree(vo_u); cudaFree(ph_u); cudaFree(wl_u); cudaFree(keys); cudaFree(keys2);
+      cudaFree(vo_u); cudaFree(ph_u); cudaFree(wl_u); cudaFree(E_u); cudaFree(keys); cudaFree(keys2);
       cudaFree(idx); cudaFree(tmp);
     };
 #define GV_SETUP_CUDA(call)                         \
@@ -332,6 +356,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_SETUP_CUDA(cudaMalloc(&vo_u, sizeof(float2) * V));
     GV_SETUP_CUDA(cudaMalloc(&ph_u, sizeof(uint4) * V));
     GV_SETUP_CUDA(cudaMalloc(&wl_u, sizeof(float) * V));
+    GV_SETUP_CUDA(cudaMalloc(&E_u, sizeof(float4) * V));
     GV_SETUP_CUDA(cudaMalloc(&keys, sizeof(unsigned long long) * V));
     GV_SETUP_CUDA(cudaMalloc(&keys2, sizeof(unsigned long long) * V));
     GV_SETUP_CUDA(cudaMalloc(&idx, sizeof(int64_t) * V));
@@ -348,7 +373,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
       const int bs = 256;
       k_prepare_vis<<<(unsigned)((ch.nvis + bs - 1) / bs), bs, 0, st>>>(
           ch.nvis, P.chans[c].off, c, ch.freq_hz, d_uvw, d_vo_in, d_w_in, P.deltau,
-          P.deltav, P.N, P.dx_rad, P.dy_rad, deg_u, vo_u, ph_u, wl_u, keys, idx);
+          P.deltav, P.N, P.dx_rad, P.dy_rad, deg_u, vo_u, ph_u, wl_u, E_u, keys, idx);
       GV_SETUP_CUDA(cudaGetLastError());
     }
     GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, idx,
@@ -360,6 +385,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_SETUP_CUDA(cudaMalloc(&P.d_vo, sizeof(float2) * V));
     GV_SETUP_CUDA(cudaMalloc(&P.d_ph, sizeof(uint4) * V));
     GV_SETUP_CUDA(cudaMalloc(&P.d_wl, sizeof(float) * V));
+    GV_SETUP_CUDA(cudaMalloc(&P.d_E, sizeof(float4) * V));
     GV_SETUP_CUDA(cudaMalloc(&P.d_cvr, sizeof(float2) * V));
     GV_SETUP_CUDA(cudaMemsetAsync(P.d_cvr, 0, sizeof(float2) * V, st));
     const unsigned gb = (unsigned)((V + 255) / 256);
@@ -367,6 +393,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     k_gather<float2><<<gb, 256, 0, st>>>(V, P.d_perm, vo_u, P.d_vo);
     k_gather<uint4><<<gb, 256, 0, st>>>(V, P.d_perm, ph_u, P.d_ph);
     k_gather<float><<<gb, 256, 0, st>>>(V, P.d_perm, wl_u, P.d_wl);
+    k_gather<float4><<<gb, 256, 0, st>>>(V, P.d_perm, E_u, P.d_E);
     GV_SETUP_CUDA(cudaGetLastError());
     // count kept visibilities per channel: keys are sorted, so the kept ones
     // of channel c are those with key < (c << 32 | 0xFFFFFFFF)
@@ -464,6 +491,42 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_CUDA(cudaMemcpy(P.d_chfreq, f.data(), sizeof(float) * C, cudaMemcpyHostToDevice));
     GV_CUDA(cudaMemcpy(P.d_ranges, r.data(), sizeof(ChanRange) * C, cudaMemcpyHostToDevice));
     GV_CUDA(cudaMemcpy(P.d_chnvis, nv.data(), sizeof(int64_t) * C, cudaMemcpyHostToDevice));
+    std::vector<int64_t> kc(C + 1, 0), k1(2 * C, 0);
+    for (int c = 0; c < C; c++) {
+      kc[c + 1] = kc[c] + P.chans[c].ngrid;
+      k1[2 * c + 1] = P.chans[c].ngrid;
+    }
+    GV_CUDA(cudaMalloc(&P.d_kc_off, sizeof(int64_t) * (C + 1)));
+    GV_CUDA(cudaMalloc(&P.d_kc_one, sizeof(int64_t) * 2 * C));
+    GV_CUDA(cudaMemcpy(P.d_kc_off, kc.data(), sizeof(int64_t) * (C + 1), cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_kc_one, k1.data(), sizeof(int64_t) * 2 * C, cudaMemcpyHostToDevice));
+  }
+  GV_CUDA(cudaMalloc(&P.d_flags, sizeof(uint32_t) * kNumFlags));
+  GV_CUDA(cudaMemsetAsync(P.d_flags, 0, sizeof(uint32_t) * kNumFlags, st));
+  {
+    const unsigned gb = (unsigned)((V + 255) / 256);
+    k_dirty_max<<<gb, 256, 0, st>>>(V, P.d_deg, P.d_vo, P.d_flags + kFlagDirtyMax);
+    GV_LAUNCH("k_dirty_max");
+  }
+  // split-K partial images of the tensor-core engine: pick the split count
+  // that fills whole waves of SMs, keeping >= 4096 visibilities per item
+  if (P.N >= 128) {
+    const int TN = P.N >= 256 ? 256 : 128;
+    const int64_t tiles = (int64_t)(P.N / 128) * (P.N / TN);
+    int64_t nmax = std::max<int64_t>(1, P.Vgrid / 4096);
+    int best = 1;
+    double best_util = -1.0;
+    for (int64_t s = 1; s <= std::min<int64_t>(nmax, 64); s++) {
+      const int64_t items = tiles * s;
+      const int64_t waves = (items + P.num_sms - 1) / P.num_sms;
+      const double util = (double)items / (double)(waves * P.num_sms);
+      if (util > best_util + 0.02) {
+        best_util = util;
+        best = (int)s;
+      }
+    }
+    P.tc_nsplit = best;
+    GV_CUDA(cudaMalloc(&P.tc_partial, sizeof(float) * (size_t)best * MN));
   }
   P.part_stride = 4 * P.num_sms;
   const int nslots = C + kMaxTerms + 8;
