@@ -1,0 +1,327 @@
+"""Benchmark: objective + gradient evaluations per second on one GB300.
+
+A step is one ObjectiveFunction::calcFunction + calcGradient pair (chi2 with
+entropy and TSV priors active, DChi2 direct-sum gradient) over the whole
+synthetic data set, i.e. one "chi2+grad evaluation" of the headline metric.
+Default workload: 2048 x 2048 image, 8 channels 225-235 GHz, 50 antennas in a
+2 km disk, 4 h at 4 s, Briggs robust 0 (35.28M visibilities), seeded
+synthetic data.
+
+  value   device-timed evaluations/s with every input resident in HBM;
+  e2e     the same through the public API (gpuvmem_gb300.Problem), the image
+          copied in from pinned host memory and the gradient and objective
+          read back every step;
+  roofline  the dominant kernel (tcgen05 DChi2) as TFLOP/s against the
+          measured dense BF16 peak / 3 (three FP16 products per algorithmic
+          multiply-add);
+  cpu_baseline  the CPU oracle (FP64 restatement of the reference's
+          algorithm) on a bounded sample, scaled to evaluations/s.
+
+--impl reference times the reference's CPU implementation of this path.  The
+reference has none (its objective and gradient exist only as CUDA kernels),
+so the arm runs the oracle port with all host threads.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from gpuvmem_gb300 import synth  # noqa: E402
+
+METRIC = "chi2+grad evals/s"
+L2_BYTES = 129 * 2 ** 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--engine", type=int, default=0)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def workload(cfg_id):
+    cfg = synth.CONFIG1 if cfg_id == 1 else synth.CONFIG0
+    terms = [("Chi2", 1.0), ("Entropy", 0.01), ("TotalSquaredVariation", 1e-4)]
+    return cfg, terms
+
+
+def config_desc(cfg, data):
+    return {"workload": f"{cfg.name}: {cfg.n}x{cfg.n} image, {len(cfg.freqs_hz)} channels, "
+                        f"{data.nvis} visibilities, {cfg.weighting} weights",
+            "image": cfg.n, "channels": len(cfg.freqs_hz), "visibilities": int(data.nvis),
+            "objective": "chi2 + entropy + TSV", "step": "objective + gradient",
+            "l2": "inputs larger than L2" if data.nvis * 56 > L2_BYTES
+                  else "L2 flushed between timed steps"}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, device=0):
+        rows = [r for r in self.rows if len(r) >= 9 and r[0] == str(device)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per DChi2 launch from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dchi2_tc_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def cpu_baseline(data, terms, sample_s, impl_kind="port"):
+    """The FP64 CPU oracle on a bounded sample: the full objective of the
+    first channel and the DChi2 sum at a few pixels, scaled to one full
+    objective + gradient evaluation over all channels and mask pixels."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    kinds = {"Chi2": O.FI_CHI2, "Entropy": O.FI_ENTROPY, "TotalSquaredVariation": O.FI_TSV}
+    oterms = [(kinds[k], lam, 0, 0, 0.001, -1.0, 1e-12) for k, lam in terms]
+    orc = O.Oracle(data, oterms)
+    img = orc.initial_image()
+    C = len(data.freqs)
+    t0 = time.time()
+    # objective: all channels in full (FFT + degrid + chi2)
+    chi0 = time.time()
+    orc.chi2(img.copy())
+    t_obj = time.time() - chi0
+    # gradient: DChi2 at a few mask pixels of channel 0 until the budget
+    mask_idx = np.flatnonzero(orc.mask.ravel())
+    rng = np.random.default_rng(0)
+    npix, t_grad = 0, 0.0
+    while t_grad < sample_s and npix < mask_idx.size:
+        pix = rng.choice(mask_idx, size=1)
+        tg = time.time()
+        orc.dchi2_pixels(0, pix)
+        t_grad += time.time() - tg
+        npix += 1
+    per_eval = t_obj + t_grad / npix * mask_idx.size * C
+    return {"value": 1.0 / per_eval, "unit": METRIC, "cores": O.lib().or_num_threads(),
+            "kind": impl_kind,
+            "sample": f"FP64 oracle: full chi2 of all {C} channels ({t_obj:.1f} s) + DChi2 at "
+                      f"{npix} of {mask_idx.size} mask pixels of channel 0 over all its "
+                      f"visibilities ({t_grad:.1f} s), scaled to the full gradient",
+            "seconds": time.time() - t0}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg, terms = workload(args.config)
+    data = synth.generate(cfg, device=None if args.config == 0 else _gen_device())
+    times = []
+    base = None
+    for s in range(args.warmup + args.steps):
+        b = cpu_baseline(data, terms, max(2.0, args.cpu_sample_s / max(1, args.steps)))
+        if s >= args.warmup:
+            times.append(1.0 / b["value"])
+            base = b
+    v = args.steps / sum(times)
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_desc(cfg, data), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": base["cores"],
+                             "kind": "port", "sample": base["sample"]},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _gen_device():
+    import torch
+    return "cuda" if torch.cuda.is_available() else None
+
+
+def run_ours(args):
+    import torch
+    import gpuvmem_gb300 as gv
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg, terms = workload(args.config)
+    data = synth.generate(cfg, device="cuda")
+    prob = gv.Problem(data, [gv.term(k, lam) for k, lam in terms], engine=args.engine)
+    stream = torch.cuda.current_stream()
+    prob.set_stream(stream.cuda_stream)
+    info = prob.info
+    img = prob.initial_image()
+    xi = torch.zeros_like(img)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    small = data.nvis * 56 <= L2_BYTES
+
+    def step():
+        f, _ = prob.objective(img)
+        prob.gradient(img, 1, xi=xi)
+        return f
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = gv.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks() as clk:
+        for s in range(args.steps):
+            if small:
+                flush.zero_()
+            ev[s][0].record(stream)
+            step()
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = (gv.launch_count() - launches0) // args.steps
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    if dist:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * args.steps / t
+
+    # DChi2 kernel alone (for the roofline): gv_dchi2 = tcgen05 kernel +
+    # split-K reduce
+    prob.chi2(img)
+    evk = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(max(2, args.steps))]
+    for a, b in evk:
+        a.record(stream)
+        prob.dchi2(img, out=xi)
+        b.record(stream)
+    torch.cuda.synchronize()
+    t_dchi2 = statistics.median(a.elapsed_time(b) for a, b in evk) / 1e3
+
+    # end to end through the public API with host buffers
+    h_img = torch.empty(img.shape, dtype=torch.float32).pin_memory()
+    h_img.copy_(img.cpu())
+    h_xi = torch.empty(img.shape, dtype=torch.float32).pin_memory()
+    d_img = torch.empty_like(img)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d_img.copy_(h_img, non_blocking=True)
+        f, _ = prob.objective(d_img)
+        prob.gradient(d_img, 1, xi=xi)
+        h_xi.copy_(xi, non_blocking=True)
+        torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    e2e = world * args.steps / t_e2e
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, src = measured_peaks()
+    peak = peaks["bf16_tflops"] / 3.0
+    V = info.nvis_in_grid
+    flops = 4.0 * cfg.n * cfg.n * V
+    achieved = flops / t_dchi2 / 1e12
+    traffic = profile_traffic()
+    cpu = cpu_baseline(data, terms, args.cpu_sample_s)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (DChi2: fp16 hi/lo x3, fp32 acc)",
+        "data": "synthetic (seeded; no public data set)", "config": config_desc(cfg, data),
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": int(img.numel() * 4),
+                "d2h_bytes_per_step": int(xi.numel() * 4 + 8 * (1 + len(terms)))},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_dchi2_tc (+ split-K reduce)",
+                     "peak_source": f"{src} dense bf16 burst {peaks['bf16_tflops']} TFLOP/s / 3",
+                     "dchi2_ms": 1e3 * t_dchi2, "algorithmic_flop": flops},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "clocks": clk.summary(local),
+        "gpu_launches": int(launches),
+        "engine": info.dchi2_engine,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -82,7 +82,7 @@ EXPORTS = ["gv_problem_create", "gv_problem_destroy", "gv_problem_info_get",
            "gv_problem_set_stream", "gv_noise_image", "gv_initial_image", "gv_chi2", "gv_dchi2",
            "gv_dchi2_channel", "gv_prior_value", "gv_prior_gradient", "gv_objective",
            "gv_gradient", "gv_optimize", "gv_dirty_image", "gv_residuals", "gv_last_error",
-           "gv_version"]
+           "gv_version", "gv_launch_count"]
 
 
 def lib():
@@ -118,10 +118,16 @@ def lib():
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    L.gv_launch_count.restype = C.c_int64
     L.gv_last_error.restype = C.c_char_p
     L.gv_version.restype = C.c_char_p
     _LIB = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(lib().gv_launch_count())
 
 
 def check(status):

@@ -4,6 +4,7 @@
 // include/classes/fi.cuh:68-81, src/mfs.cu:117-140).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -18,6 +19,9 @@ struct gv_problem {
 namespace gv {
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -255,6 +259,8 @@ gv_status gv_residuals(gv_problem* p, float* h_out) {
 }
 
 const char* gv_last_error(void) { return gv::g_last_error.c_str(); }
+
+int64_t gv_launch_count(void) { return (int64_t)gv::g_launches.load(); }
 
 const char* gv_version(void) { return "gpuvmem_gb300 0.1 (sm_103a)"; }
 

@@ -134,8 +134,12 @@ gv_status cuda_fail(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return ::gv::cuda_fail(_e, #call); \
   } while (0)
 
+// Counts every kernel launch of the library (gv_launch_count) and turns a
+// launch error into a status.
+void count_launch();
 #define GV_LAUNCH(what)                                         \
   do {                                                          \
+    ::gv::count_launch();                                       \
     cudaError_t _e = cudaGetLastError();                        \
     if (_e != cudaSuccess) return ::gv::cuda_fail(_e, what);     \
   } while (0)

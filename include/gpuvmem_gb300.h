@@ -205,6 +205,9 @@ gv_status gv_residuals(gv_problem* p, float* h_out);
 
 const char* gv_last_error(void);
 const char* gv_version(void);
+/* Diagnostics (no counterpart in the reference): number of kernels the
+ * library has launched in this process. */
+int64_t gv_launch_count(void);
 
 #ifdef __cplusplus
 }

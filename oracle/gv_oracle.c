@@ -407,6 +407,31 @@ void or_dchi2_channel(const or_problem* p, int c, const double* vr,
     }
 }
 
+void or_dchi2_pixels(const or_problem* p, int c, const double* vr, int npix,
+                     const int64_t* pix, double* out) {
+  const int64_t o = p->chan_off[c], n = p->chan_off[c + 1] - o;
+  const int x0 = (int)p->xobs, y0 = (int)p->yobs;
+  for (int t = 0; t < npix; t++) {
+    const int i = (int)(pix[t] / p->N), j = (int)(pix[t] % p->N);
+    const double x = (j - x0) * p->DELTAX * OR_RPDEG_D;
+    const double y = (i - y0) * p->DELTAY * OR_RPDEG_D;
+    const double zm1 = sqrt(1.0 - x * x - y * y) - 1.0;
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s)
+    for (int64_t k = 0; k < n; k++) {
+      const int64_t g = o + k;
+      const double w = p->weight[g];
+      if (w == 0.0) continue;
+      const double ph = 2.0 * OR_PI_D *
+                        (x * p->uvw[3 * g] + y * p->uvw[3 * g + 1] + zm1 * p->uvw[3 * g + 2]);
+      double sn, cs;
+      sincos(ph, &sn, &cs);
+      s += w * (vr[2 * g] * cs + vr[2 * g + 1] * sn);
+    }
+    out[t] = s;
+  }
+}
+
 /* dchi2(), src/functions.cu:4456-4558, with DChi2_total_I_nu_0 /
  * DChi2_total_alpha, src/functions.cu:3968-4024 */
 void or_dchi2(const or_problem* p, const float* img, const double* vr,

@@ -118,6 +118,9 @@ void or_dchi2(const or_problem* p, const float* img, const double* vr,
 /* raw DChi2 of one channel: out[M*N] = -fg*A*sum_k w Re(conj(Vr) e^{i phi}) */
 void or_dchi2_channel(const or_problem* p, int c, const double* vr,
                       double* out);
+/* raw DChi2 sum of channel c at npix pixels (flat indices), FP64 */
+void or_dchi2_pixels(const or_problem* p, int c, const double* vr, int npix,
+                     const int64_t* pix, double* out);
 double or_prior_value(const or_problem* p, const or_term* t, const float* img);
 void or_prior_grad(const or_problem* p, const or_term* t, const float* img,
                    double* out /* [M*N] */);

@@ -82,6 +82,7 @@ def lib():
         L.or_model_vis.argtypes = [P, f32p, f64p]
         L.or_dchi2.argtypes = [P, f32p, f64p, C.c_int, f64p]
         L.or_dchi2_channel.argtypes = [P, C.c_int, f64p, f64p]
+        L.or_dchi2_pixels.argtypes = [P, C.c_int, f64p, C.c_int, C.POINTER(C.c_int64), f64p]
         L.or_prior_value.argtypes = [P, C.POINTER(OrTerm), f32p]
         L.or_prior_value.restype = C.c_double
         L.or_prior_grad.argtypes = [P, C.POINTER(OrTerm), f32p, f64p]
@@ -195,6 +196,13 @@ class Oracle:
         out = np.zeros(self.M * self.N, dtype=np.float64)
         lib().or_dchi2_channel(C.byref(self.prob), c, _p(self.vr, C.c_double), _p(out, C.c_double))
         return out.reshape(self.N, self.M)
+
+    def dchi2_pixels(self, c, pix):
+        pix = np.ascontiguousarray(pix, dtype=np.int64)
+        out = np.zeros(pix.size, dtype=np.float64)
+        lib().or_dchi2_pixels(C.byref(self.prob), c, _p(self.vr, C.c_double), pix.size,
+                              _p(pix, C.c_int64), _p(out, C.c_double))
+        return out
 
     def prior_value(self, ti, img):
         img = np.ascontiguousarray(img, dtype=np.float32)
