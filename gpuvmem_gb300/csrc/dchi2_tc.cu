@@ -12,25 +12,33 @@
 // i.e. a real GEMM D = A B with K = 2V:  A[i][2k] = Re b, A[i][2k+1] = Im b,
 // B[2k][j] = Re x, B[2k+1][j] = -Im x.
 //
-// Operands are never materialised in HBM.  Per chunk of 32 visibilities the
-// CTA's 8 warps generate the 128 x 64 A tile and the TN x 64 B tile in
+// Operands are never materialised in HBM.  Per chunk of 32 visibilities,
+// 16 generator warps build the 128 x 64 A tile and the TN x 64 B tile in
 // shared memory: each thread produces 8 consecutive rows for one
 // visibility from an exact fixed-point anchor (the linear phase is reduced
 // mod 1 with 32-bit integer products) and a chirp recurrence in FP32.  Each
 // operand is split into FP16 hi + lo parts and the tile is accumulated with
 // three MMAs (hi*hi + hi*lo + lo*hi) into an FP32 accumulator in TMEM.
-// Operand tiles are MN-major with the 128-byte swizzle; two stages let the
-// tensor core work on chunk n while the warps generate chunk n+1.  Every
-// 16 chunks the accumulator is drained into a running sum held in the other
-// half of TMEM (short FP32 accumulation chains); at the end of each channel
-// the running sum is multiplied by the channel's epilogue factor (beam,
-// fg_scale, chain rule) and added to this split's partial image.  Split-K
-// partials are summed in FP64 in a fixed order, so results are
+// Operand tiles are MN-major with the 128-byte swizzle.
+//
+// Warp roles (no block-wide barrier per chunk):
+//   warps 0..15  generators: wait for the chunk's visibility constants and
+//                a free operand stage, generate, arrive on the stage's
+//                "full" barrier; every kSlab chunks (and at the end of a
+//                channel) they drain the accumulator into a running sum in
+//                the other half of TMEM, and at the end of a channel apply
+//                the channel's epilogue factor (beam, fg_scale, chain rule)
+//                and add it to this split's partial image;
+//   warp 16      control: its lanes load the visibility constants of
+//                chunks up to three ahead into a 4-slot ring; its lane 0
+//                issues the MMAs of each full stage and commits them to the
+//                stage's "empty" barrier.
+// Split-K partials are summed in FP64 in a fixed order, so results are
 // deterministic.
 //
-// Every wait on an mbarrier is bounded: on timeout the kernel records an
-// error word, stops issuing work, waits (bounded) for its own MMAs, frees
-// its TMEM and returns; the host turns the word into GV_ERR_DEVICE.
+// Every wait is bounded: on timeout the kernel records an error word, every
+// warp stops, the MMAs in flight are waited for (bounded), TMEM is freed and
+// the kernel returns; the host turns the word into GV_ERR_DEVICE.
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -41,11 +49,15 @@ namespace gv {
 
 namespace tc {
 
-constexpr int kTM = 128;          // image rows per tile (MMA M)
-constexpr int kChunkVis = 32;     // visibilities per chunk
+constexpr int kTM = 128;            // image rows per tile (MMA M)
+constexpr int kChunkVis = 32;       // visibilities per chunk
 constexpr int kKC = 2 * kChunkVis;  // K elements per chunk
-constexpr int kThreads = 256;
-constexpr int kSlab = 16;         // chunks accumulated before a drain
+constexpr int kGenWarps = 16;
+constexpr int kGenThreads = kGenWarps * 32;
+constexpr int kThreads = kGenThreads + 32;
+constexpr int kVisSlots = 4;
+constexpr int kLookahead = kVisSlots - 1;
+constexpr int kSlab = 16;           // chunks accumulated before a drain
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -68,6 +80,9 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* m) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -79,11 +94,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity) {
+// bounded wait; returns false on timeout or when another warp gave up
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, volatile int* abort,
+                                          uint32_t* err, uint32_t code) {
   const long long t0 = clock64();
   while (!mbar_try_wait(m, parity)) {
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (*abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      atomicExch(err, code);
+      *abort = 1;
+      return false;
+    }
   }
   return true;
 }
@@ -181,27 +202,27 @@ __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
          ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// byte offset of element (row m, k-index kk) in an MN-major 128B-swizzled
-// tile whose MN atoms (64 rows) are 1024 B apart and K atoms (8 rows) are
-// sbo apart; the 16-byte chunk holds rows 8*oct .. 8*oct+7.
+// byte offset of the 16-byte chunk holding rows 8*oct..8*oct+7 of MN atom
+// `matom` at K index kk, in an MN-major 128B-swizzled tile whose MN atoms
+// (64 rows) are 1024 B apart and K atoms (8 rows) are sbo apart
 __device__ __forceinline__ uint32_t tile_off(int matom, int oct, int kk, uint32_t sbo) {
   const int katom = kk >> 3, krow = kk & 7;
   return (uint32_t)(katom * sbo + matom * 1024 + krow * 128 + ((oct ^ krow) << 4));
 }
 
 struct TcParams {
-  int N;           // image is N x N
+  int N;  // image is N x N
   int64_t MN;
-  int x0, y0;      // int-truncated centre (DChi2 coordinates)
+  int x0, y0;  // int-truncated centre (DChi2 coordinates)
   float xobs, yobs, nu_0, D, pbf, pbcut, fg_scale, threshold;
   int pb;
   double DELTAX, DELTAY;
   int normalize, flag_opt, mode;
   int ntile_i, ntile_j, nsplit;
   int C;
-  int64_t Ktot;                  // kept visibilities over all channels
-  const int64_t* kc_off;         // [C+1] compact offsets of kept visibilities
-  const ChanRange* ranges;       // [C]
+  int64_t Ktot;               // kept visibilities over all channels
+  const int64_t* kc_off;      // [C+1] compact offsets of kept visibilities
+  const ChanRange* ranges;    // [C]
   const float* chfreq;
   const int64_t* chnvis;
   const uint4* ph;
@@ -211,20 +232,21 @@ struct TcParams {
   const float2* vo;
   const uint8_t* mask;
   const float* img;
-  const uint32_t* cmax_bits;     // max |c| (float bits)
-  float* partial;                // [nsplit][MN]
+  const uint32_t* cmax_bits;  // max |c| (float bits)
+  float* partial;             // [nsplit][MN]
   uint32_t* err;
 };
 
 template <int TN>
 struct Layout {
-  static constexpr uint32_t kSboA = (kTM / 64) * 1024;   // bytes between K atoms of A
+  static constexpr uint32_t kSboA = (kTM / 64) * 1024;  // bytes between K atoms of A
   static constexpr uint32_t kSboB = (TN / 64) * 1024;
   static constexpr uint32_t kTileA = kSboA * (kKC / 8);  // one A part (hi or lo)
   static constexpr uint32_t kTileB = kSboB * (kKC / 8);
   static constexpr uint32_t kStage = 2 * kTileA + 2 * kTileB;
-  static constexpr uint32_t kVis = 2 * kChunkVis * sizeof(VisEntry);
-  static constexpr uint32_t kSmem = 1024 + 2 * kStage + kVis + 64;
+  static constexpr uint32_t kVis = kVisSlots * kChunkVis * sizeof(VisEntry);
+  static constexpr uint32_t kBars = 16 * 8;
+  static constexpr uint32_t kSmem = 1024 + 2 * kStage + kVis + kBars + 16;
 };
 
 // Epilogue factor of one pixel for channel c (mode 0: gradient with chain
@@ -263,10 +285,11 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
   sincospif(2.0f * th, &sn, &cs);
   float2 v = make_float2(cs, sn);
   if (kIsB) v = cmul(v, ve.c);
+  // d = e^{2 pi i (f - G (2 r0 + 1))}, q = e^{-4 pi i G}; the chirp angles
+  // are below 1e-3 rad, so second-order expansions are exact in FP32
   const float eps = -6.283185307179586f * G * (2.0f * rf + 1.0f);
-  float2 d = cmul(E, make_float2(1.0f - 0.5f * eps * eps, eps));
+  float2 d = cmul(E, make_float2(fmaf(-0.5f * eps, eps, 1.0f), eps));
   const float eq = -12.566370614359172f * G;
-  const float2 q = make_float2(1.0f - 0.5f * eq * eq, eq);
   float re[8], im[8];
 #pragma unroll
   for (int t = 0; t < 8; t++) {
@@ -274,7 +297,7 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
     im[t] = kIsB ? -v.y : v.y;
     if (t < 7) {
       v = cmul(v, d);
-      d = cmul(d, q);
+      d = make_float2(fmaf(-eq, d.y, d.x), fmaf(eq, d.x, d.y));
     }
   }
   uint32_t hre[4], him[4], lre[4], lim[4];
@@ -299,17 +322,69 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
   *reinterpret_cast<uint4*>(lo + oim) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
 }
 
+// The chunk sequence every warp walks in the same order: work items
+// (tile, split) owned by this CTA, the channels each split overlaps, and
+// 32-visibility chunks within a channel.
+struct ChunkIter {
+  int item, c, n, nchunks;
+  int64_t goff, nvis;
+  bool valid;
+};
+
+__device__ __forceinline__ void item_range(const TcParams& p, int item, int64_t* ks,
+                                           int64_t* ke) {
+  const int split = item % p.nsplit;
+  *ks = p.Ktot * split / p.nsplit;
+  *ke = p.Ktot * (split + 1) / p.nsplit;
+}
+
+// position `it` on the first chunk at or after (item, channel c); returns
+// false when the CTA has no more chunks
+__device__ bool iter_seek(const TcParams& p, int nitems, ChunkIter& it) {
+  while (it.item < nitems) {
+    int64_t ks, ke;
+    item_range(p, it.item, &ks, &ke);
+    for (; it.c < p.C; it.c++) {
+      const int64_t cs = p.kc_off[it.c], ce = p.kc_off[it.c + 1];
+      const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
+      if (a < b) {
+        it.goff = p.ranges[it.c].off + (a - cs);
+        it.nvis = b - a;
+        it.nchunks = (int)((it.nvis + kChunkVis - 1) / kChunkVis);
+        it.n = 0;
+        it.valid = true;
+        return true;
+      }
+    }
+    it.item += gridDim.x;
+    it.c = 0;
+  }
+  it.valid = false;
+  return false;
+}
+
+__device__ __forceinline__ void iter_next(const TcParams& p, int nitems, ChunkIter& it) {
+  if (++it.n < it.nchunks) return;
+  it.c++;
+  iter_seek(p, nitems, it);
+}
+
 template <int TN>
 __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   using L = Layout<TN>;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  uint8_t* stage_ptr[2] = {base, base + L::kStage};
   VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + 2 * L::kStage);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
+  uint64_t* op_full = bars;                  // [2]  count kGenThreads
+  uint64_t* op_empty = bars + 2;             // [2]  tcgen05.commit
+  uint64_t* vis_full = bars + 4;             // [4]  count 32 (control lanes)
+  uint64_t* vis_empty = bars + 8;            // [4]  count kGenThreads
+  uint64_t* drained = bars + 12;             // [1]  count kGenThreads
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 16);
   __shared__ int s_abort;
+  volatile int* abort = &s_abort;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
@@ -317,8 +392,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
     tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    mbar_init(&op_full[0], kGenThreads);
+    mbar_init(&op_full[1], kGenThreads);
+    mbar_init(&op_empty[0], 1);
+    mbar_init(&op_empty[1], 1);
+    for (int s = 0; s < kVisSlots; s++) {
+      mbar_init(&vis_full[s], 32);
+      mbar_init(&vis_empty[s], kGenThreads);
+    }
+    mbar_init(drained, kGenThreads);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -335,111 +417,79 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   if (cmax > 0.0f) frexpf(cmax, &e);
   const float scale = ldexpf(1.0f, -e);
   const float inv_s = ldexpf(1.0f, e);
-  const uint32_t idesc = make_idesc(kTM, TN);
-
-  // drain / epilogue geometry: warp -> 32 TMEM lanes and a column half
-  const int lq = warp & 3, half = warp >> 2;
-  constexpr int kColsPerThread = TN / 2;
-  const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
-
-  uint32_t nch = 0;  // chunks issued by this CTA (stage = nch & 1)
-  bool ok = true;
   const int nitems = p.ntile_i * p.ntile_j * p.nsplit;
-  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-    const int split = item % p.nsplit;
-    const int tile = item / p.nsplit;
-    const int ti = tile / p.ntile_j, tj = tile % p.ntile_j;
-    const int i0 = ti * kTM, j0 = tj * TN;
-    const int64_t ks = p.Ktot * split / p.nsplit, ke = p.Ktot * (split + 1) / p.nsplit;
-    bool first_channel = true;
-    // this thread's epilogue pixels
-    const int ei = i0 + 32 * lq + lane;
-    const int ej0 = j0 + half * kColsPerThread;
-    float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + ej0;
-    for (int c = 0; c < p.C && ok; c++) {
-      const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
-      const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
-      if (a >= b) continue;
-      const int64_t goff = p.ranges[c].off + (a - cs);
-      const int64_t nvis = b - a;
-      const int nchunks = (int)((nvis + kChunkVis - 1) / kChunkVis);
-      bool run_empty = true;
-      for (int n = 0; n < nchunks && ok; n++) {
-        const int st = nch & 1;
-        uint8_t* sp = stage_ptr[st];
-        if (nch >= 2) {
-          if (!mbar_wait(&mbar[st], ((nch >> 1) - 1) & 1)) {
-            atomicExch(p.err, 1u);
-            s_abort = 1;
-          }
+  uint32_t nch = 0;  // position in this CTA's chunk sequence
+
+  if (warp == kGenWarps) {
+    // ------------------------------- control warp --------------------------
+    ChunkIter ld{(int)blockIdx.x, 0, 0, 0, 0, 0, false};
+    ChunkIter mm = ld;
+    iter_seek(p, nitems, ld);
+    iter_seek(p, nitems, mm);
+    uint32_t nld = 0, ndrain = 0;
+    const uint32_t idesc = make_idesc(kTM, TN);
+    bool ok = true;
+    auto load_one = [&](const ChunkIter& it, uint32_t q) -> bool {
+      const int slot = q % kVisSlots;
+      if (q >= kVisSlots) {
+        if (!mbar_wait(&vis_empty[slot], ((q / kVisSlots) - 1) & 1, abort, p.err, 4u)) return false;
+      }
+      VisEntry ve;
+      const int64_t kidx = (int64_t)it.n * kChunkVis + lane;
+      if (kidx < it.nvis) {
+        const int64_t g = it.goff + kidx;
+        const uint4 ph = p.ph[g];
+        const float4 E = p.E[g];
+        float2 cc;
+        if (p.mode == 2) {
+          const float4 d = p.deg[g];
+          const float2 o = p.vo[g];
+          cc = make_float2(d.w * o.x, -(d.w * o.y));
+        } else {
+          const float2 r = p.cvr[g];
+          cc = make_float2(r.x, -r.y);
         }
-        __syncthreads();
-        if (s_abort) {
-          ok = false;
-          break;
-        }
-        // stage the chunk's per-visibility constants
-        if (tid < kChunkVis) {
-          VisEntry ve;
-          const int64_t kidx = (int64_t)n * kChunkVis + tid;
-          if (kidx < nvis) {
-            const int64_t g = goff + kidx;
-            const uint4 ph = p.ph[g];
-            const float4 E = p.E[g];
-            float2 cc;
-            if (p.mode == 2) {
-              const float4 d = p.deg[g];
-              const float2 o = p.vo[g];
-              cc = make_float2(d.w * o.x, -(d.w * o.y));
-            } else {
-              const float2 r = p.cvr[g];
-              cc = make_float2(r.x, -r.y);
-            }
-            ve.FU = ph.x;
-            ve.FV = ph.y;
-            ve.GU = __uint_as_float(ph.z);
-            ve.GV = __uint_as_float(ph.w);
-            ve.Eu = make_float2(E.x, E.y);
-            ve.Ev = make_float2(E.z, E.w);
-            ve.c = make_float2(cc.x * scale, cc.y * scale);
-          } else {
-            ve.FU = ve.FV = 0u;
-            ve.GU = ve.GV = 0.0f;
-            ve.Eu = ve.Ev = make_float2(1.0f, 0.0f);
-            ve.c = make_float2(0.0f, 0.0f);
-          }
-          s_vis[st * kChunkVis + tid] = ve;
-        }
-        __syncthreads();
-        // generate: A (image rows) 2 atoms x 8 visibility quads, then B
-        uint8_t* a_hi = sp;
-        uint8_t* a_lo = sp + L::kTileA;
-        uint8_t* b_hi = sp + 2 * L::kTileA;
-        uint8_t* b_lo = sp + 2 * L::kTileA + L::kTileB;
-        const int oct = lane & 7, kq = lane >> 3;
-        constexpr int kTasksA = (kTM / 64) * (kChunkVis / 4);
-        constexpr int kTasksB = (TN / 64) * (kChunkVis / 4);
-        for (int wt = warp; wt < kTasksA + kTasksB; wt += kThreads / 32) {
-          if (wt < kTasksA) {
-            const int matom = wt / (kChunkVis / 4);
-            const int kv = (wt % (kChunkVis / 4)) * 4 + kq;
-            const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
-            gen_octet<false>(s_vis[st * kChunkVis + kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA);
-          } else {
-            const int w2 = wt - kTasksA;
-            const int matom = w2 / (kChunkVis / 4);
-            const int kv = (w2 % (kChunkVis / 4)) * 4 + kq;
-            const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
-            gen_octet<true>(s_vis[st * kChunkVis + kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB);
-          }
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        ve.FU = ph.x;
+        ve.FV = ph.y;
+        ve.GU = __uint_as_float(ph.z);
+        ve.GV = __uint_as_float(ph.w);
+        ve.Eu = make_float2(E.x, E.y);
+        ve.Ev = make_float2(E.z, E.w);
+        ve.c = make_float2(cc.x * scale, cc.y * scale);
+      } else {
+        ve.FU = ve.FV = 0u;
+        ve.GU = ve.GV = 0.0f;
+        ve.Eu = ve.Ev = make_float2(1.0f, 0.0f);
+        ve.c = make_float2(0.0f, 0.0f);
+      }
+      s_vis[slot * kChunkVis + lane] = ve;
+      mbar_arrive(&vis_full[slot]);
+      return true;
+    };
+    // prime the ring
+    while (ok && ld.valid && nld < (uint32_t)kLookahead) {
+      ok = load_one(ld, nld);
+      nld++;
+      iter_next(p, nitems, ld);
+    }
+    while (ok && mm.valid) {
+      if (ld.valid) {
+        ok = load_one(ld, nld);
+        nld++;
+        iter_next(p, nitems, ld);
+        if (!ok) break;
+      }
+      const int st = nch & 1;
+      const bool fresh = (mm.n % kSlab) == 0;
+      const bool drain = (mm.n == mm.nchunks - 1) || ((mm.n % kSlab) == kSlab - 1);
+      if (lane == 0) {
+        ok = mbar_wait(&op_full[st], (nch >> 1) & 1, abort, p.err, 5u);
+        if (ok && fresh && nch > 0) ok = mbar_wait(drained, (ndrain - 1) & 1, abort, p.err, 6u);
+        if (ok) {
           fence_after();
-          const uint32_t sa_hi = smem_u32(a_hi), sa_lo = smem_u32(a_lo);
-          const uint32_t sb_hi = smem_u32(b_hi), sb_lo = smem_u32(b_lo);
-          const bool fresh = (n % kSlab) == 0;
+          uint8_t* sp = base + st * L::kStage;
+          const uint32_t sa_hi = smem_u32(sp), sa_lo = sa_hi + L::kTileA;
+          const uint32_t sb_hi = sa_hi + 2 * L::kTileA, sb_lo = sb_hi + L::kTileB;
 #pragma unroll
           for (int t = 0; t < kKC / 16; t++) {
             const uint64_t ah = make_desc(sa_hi + t * 2 * L::kSboA, 1024, L::kSboA);
@@ -450,27 +500,93 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
             mma_f16(t_acc, ah, bl, idesc, 1u);
             mma_f16(t_acc, al, bh, idesc, 1u);
           }
-          mma_commit(&mbar[st]);
+          mma_commit(&op_empty[st]);
         }
-        const bool last = (n == nchunks - 1);
-        const bool drain = last || ((n % kSlab) == kSlab - 1);
-        const uint32_t my_commit = nch >> 1;
-        nch++;
-        if (drain) {
-          if (!mbar_wait(&mbar[st], my_commit & 1)) {
-            atomicExch(p.err, 2u);
-            s_abort = 1;
+      }
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (drain) ndrain++;
+      nch++;
+      iter_next(p, nitems, mm);
+    }
+    // retire: no MMA may be in flight when TMEM is freed
+    if (lane == 0 && nch > 0) {
+      const uint32_t q = nch - 1;
+      const long long t0 = clock64();
+      while (!mbar_try_wait(&op_empty[q & 1], (q >> 1) & 1)) {
+        if (clock64() - t0 > kWaitCycles) {
+          atomicExch(p.err, 7u);
+          break;
+        }
+      }
+    }
+  } else {
+    // ----------------------------- generator warps -------------------------
+    const int oct = lane & 7, kq = lane >> 3;
+    constexpr int kVq = kChunkVis / 4;  // visibility quads per chunk
+    constexpr int kTasksA = (kTM / 64) * kVq;
+    constexpr int kTasksB = (TN / 64) * kVq;
+    constexpr int kCols = TN / 4;       // epilogue columns per thread
+    const int lq = warp & 3, cg = warp >> 2;
+    const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      const int split = item % p.nsplit;
+      const int tile = item / p.nsplit;
+      const int ti = tile / p.ntile_j, tj = tile % p.ntile_j;
+      const int i0 = ti * kTM, j0 = tj * TN;
+      int64_t ks, ke;
+      item_range(p, item, &ks, &ke);
+      bool first_channel = true;
+      const int ei = i0 + 32 * lq + lane;
+      const int ej0 = j0 + cg * kCols;
+      float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + ej0;
+      for (int c = 0; c < p.C && ok; c++) {
+        const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
+        const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
+        if (a >= b) continue;
+        const int nchunks = (int)((b - a + kChunkVis - 1) / kChunkVis);
+        bool run_empty = true;
+        for (int n = 0; n < nchunks && ok; n++) {
+          const int st = nch & 1;
+          const int slot = nch % kVisSlots;
+          if (nch >= 2) ok = mbar_wait(&op_empty[st], ((nch >> 1) - 1) & 1, abort, p.err, 1u);
+          if (ok) ok = mbar_wait(&vis_full[slot], (nch / kVisSlots) & 1, abort, p.err, 2u);
+          if (!ok) break;
+          uint8_t* sp = base + st * L::kStage;
+          uint8_t* a_hi = sp;
+          uint8_t* a_lo = sp + L::kTileA;
+          uint8_t* b_hi = sp + 2 * L::kTileA;
+          uint8_t* b_lo = sp + 2 * L::kTileA + L::kTileB;
+          const VisEntry* sv = s_vis + slot * kChunkVis;
+          for (int wt = warp; wt < kTasksA + kTasksB; wt += kGenWarps) {
+            if (wt < kTasksA) {
+              const int matom = wt / kVq;
+              const int kv = (wt % kVq) * 4 + kq;
+              const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
+              gen_octet<false>(sv[kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA);
+            } else {
+              const int w2 = wt - kTasksA;
+              const int matom = w2 / kVq;
+              const int kv = (w2 % kVq) * 4 + kq;
+              const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
+              gen_octet<true>(sv[kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB);
+            }
           }
-          __syncthreads();
-          if (s_abort) {
-            ok = false;
-            break;
-          }
+          fence_proxy_async();
+          mbar_arrive(&op_full[st]);
+          mbar_arrive(&vis_empty[slot]);
+          const bool last = (n == nchunks - 1);
+          const bool drain = last || ((n % kSlab) == kSlab - 1);
+          const uint32_t my = nch;
+          nch++;
+          if (!drain) continue;
+          ok = mbar_wait(&op_empty[my & 1], (my >> 1) & 1, abort, p.err, 3u);
+          if (!ok) break;
           fence_after();
           // running sum += accumulator (short FP32 chains)
 #pragma unroll 1
-          for (int cb = 0; cb < kColsPerThread; cb += 32) {
-            const uint32_t col = (uint32_t)(half * kColsPerThread + cb);
+          for (int cb = 0; cb < kCols; cb += 32) {
+            const uint32_t col = (uint32_t)(cg * kCols + cb);
             float acc[32], run[32];
             tmem_ld32(t_acc + lane_off + col, acc);
             if (!run_empty) {
@@ -481,11 +597,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
             tmem_st32(t_run + lane_off + col, acc);
           }
           run_empty = false;
+          fence_before();
+          mbar_arrive(drained);
           if (last) {
             // channel epilogue: partial (+)= factor * running sum
 #pragma unroll 1
-            for (int cb = 0; cb < kColsPerThread; cb += 32) {
-              const uint32_t col = (uint32_t)(half * kColsPerThread + cb);
+            for (int cb = 0; cb < kCols; cb += 32) {
+              const uint32_t col = (uint32_t)(cg * kCols + cb);
               float run[32];
               tmem_ld32(t_run + lane_off + col, run);
 #pragma unroll 4
@@ -500,21 +618,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
             }
             first_channel = false;
           }
-          fence_before();
-          __syncthreads();
         }
       }
+      if (ok && first_channel) {
+        // no visibilities in this split for this tile: its partial is zero
+        for (int k = 0; k < kCols; k++) prow[k] = 0.0f;
+      }
     }
-    if (ok && first_channel) {
-      // no visibilities in this split for this tile: its partial is zero
-      for (int k = 0; k < kColsPerThread; k++) prow[k] = 0.0f;
-    }
-  }
-  // retire: make sure no MMA is still reading shared memory / writing TMEM
-  if (nch > 0) {
-    const uint32_t st = (nch - 1) & 1;
-    const uint32_t last_commit = (nch - 1) >> 1;
-    if (!mbar_wait(&mbar[st], last_commit & 1)) atomicExch(p.err, 3u);
   }
   fence_before();
   __syncthreads();

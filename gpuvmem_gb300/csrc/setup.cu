@@ -509,14 +509,14 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_LAUNCH("k_dirty_max");
   }
   // split-K partial images of the tensor-core engine: pick the split count
-  // that fills whole waves of SMs, keeping >= 4096 visibilities per item
+  // that fills whole waves of SMs, keeping >= 1024 visibilities per item
   if (P.N >= 128) {
     const int TN = P.N >= 256 ? 256 : 128;
     const int64_t tiles = (int64_t)(P.N / 128) * (P.N / TN);
-    int64_t nmax = std::max<int64_t>(1, P.Vgrid / 4096);
+    int64_t nmax = std::max<int64_t>(1, P.Vgrid / 1024);
     int best = 1;
     double best_util = -1.0;
-    for (int64_t s = 1; s <= std::min<int64_t>(nmax, 64); s++) {
+    for (int64_t s = 1; s <= std::min<int64_t>(nmax, 256); s++) {
       const int64_t items = tiles * s;
       const int64_t waves = (items + P.num_sms - 1) / P.num_sms;
       const double util = (double)items / (double)(waves * P.num_sms);
