@@ -97,16 +97,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
 // bounded wait; returns false on timeout or when another warp gave up
 __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, volatile int* abort,
                                           uint32_t* err, uint32_t code) {
+  if (mbar_try_wait(m, parity)) return true;
   const long long t0 = clock64();
-  while (!mbar_try_wait(m, parity)) {
-    if (*abort) return false;
-    if (clock64() - t0 > kWaitCycles) {
-      atomicExch(err, code);
-      *abort = 1;
-      return false;
+  for (uint32_t it = 1;; it++) {
+    if (mbar_try_wait(m, parity)) return true;
+    if ((it & 15) == 0) {
+      if (*abort) return false;
+      if (clock64() - t0 > kWaitCycles) {
+        atomicExch(err, code);
+        *abort = 1;
+        return false;
+      }
     }
   }
-  return true;
+}
+// warp-level wait: lane 0 waits, the warp reconverges (memory ordering of
+// __syncwarp carries lane 0's acquire to the other lanes)
+__device__ __forceinline__ bool warp_wait(uint64_t* m, uint32_t parity, volatile int* abort,
+                                          uint32_t* err, uint32_t code) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(m, parity, abort, err, code) ? 1 : 0;
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+// warp-level arrive (barriers counted in warps)
+__device__ __forceinline__ void warp_arrive(uint64_t* m) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(m);
 }
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -218,6 +234,7 @@ struct TcParams {
   int pb;
   double DELTAX, DELTAY;
   int normalize, flag_opt, mode;
+  int fast_anchor;  // 1: anchor phasor from the SFU (__sincosf), 0: sincospif
   int ntile_i, ntile_j, nsplit;
   int C;
   int64_t Ktot;               // kept visibilities over all channels
@@ -273,7 +290,7 @@ __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int
 // the FP16 hi/lo parts of Re and (sign-adjusted) Im.
 template <bool kIsB>
 __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* hi, uint8_t* lo,
-                                          int matom, int oct, int kv, uint32_t sbo) {
+                                          int matom, int oct, int kv, uint32_t sbo, bool fast) {
   const uint32_t F = kIsB ? ve.FU : ve.FV;
   const float G = kIsB ? ve.GU : ve.GV;
   const float2 E = kIsB ? ve.Eu : ve.Ev;
@@ -281,8 +298,13 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
   const uint32_t lin = (uint32_t)r0 * F;
   float th = (float)(int32_t)lin * 2.3283064365386963e-10f;
   th = fmaf(-rf * rf, G, th);
+  // th is in [-0.5, 0.5] cycles: the SFU's sin/cos of 2 pi th are within
+  // ~4e-7 absolute, below the FP16 hi/lo split's own error budget
   float sn, cs;
-  sincospif(2.0f * th, &sn, &cs);
+  if (fast)
+    __sincosf(6.283185307179586f * th, &sn, &cs);
+  else
+    sincospif(2.0f * th, &sn, &cs);
   float2 v = make_float2(cs, sn);
   if (kIsB) v = cmul(v, ve.c);
   // d = e^{2 pi i (f - G (2 r0 + 1))}, q = e^{-4 pi i G}; the chirp angles
@@ -377,11 +399,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
   VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + 2 * L::kStage);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
-  uint64_t* op_full = bars;                  // [2]  count kGenThreads
+  uint64_t* op_full = bars;                  // [2]  one arrive per generator warp
   uint64_t* op_empty = bars + 2;             // [2]  tcgen05.commit
   uint64_t* vis_full = bars + 4;             // [4]  count 32 (control lanes)
-  uint64_t* vis_empty = bars + 8;            // [4]  count kGenThreads
-  uint64_t* drained = bars + 12;             // [1]  count kGenThreads
+  uint64_t* vis_empty = bars + 8;            // [4]  one arrive per generator warp
+  uint64_t* drained = bars + 12;             // [1]  one arrive per generator warp
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 16);
   __shared__ int s_abort;
   volatile int* abort = &s_abort;
@@ -392,15 +414,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
     tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(&op_full[0], kGenThreads);
-    mbar_init(&op_full[1], kGenThreads);
+    mbar_init(&op_full[0], kGenWarps);
+    mbar_init(&op_full[1], kGenWarps);
     mbar_init(&op_empty[0], 1);
     mbar_init(&op_empty[1], 1);
     for (int s = 0; s < kVisSlots; s++) {
       mbar_init(&vis_full[s], 32);
-      mbar_init(&vis_empty[s], kGenThreads);
+      mbar_init(&vis_empty[s], kGenWarps);
     }
-    mbar_init(drained, kGenThreads);
+    mbar_init(drained, kGenWarps);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -522,6 +544,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   } else {
     // ----------------------------- generator warps -------------------------
     const int oct = lane & 7, kq = lane >> 3;
+    const bool fast = p.fast_anchor != 0;
     constexpr int kVq = kChunkVis / 4;  // visibility quads per chunk
     constexpr int kTasksA = (kTM / 64) * kVq;
     constexpr int kTasksB = (TN / 64) * kVq;
@@ -549,8 +572,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         for (int n = 0; n < nchunks && ok; n++) {
           const int st = nch & 1;
           const int slot = nch % kVisSlots;
-          if (nch >= 2) ok = mbar_wait(&op_empty[st], ((nch >> 1) - 1) & 1, abort, p.err, 1u);
-          if (ok) ok = mbar_wait(&vis_full[slot], (nch / kVisSlots) & 1, abort, p.err, 2u);
+          if (nch >= 2) ok = warp_wait(&op_empty[st], ((nch >> 1) - 1) & 1, abort, p.err, 1u);
+          if (ok) ok = warp_wait(&vis_full[slot], (nch / kVisSlots) & 1, abort, p.err, 2u);
           if (!ok) break;
           uint8_t* sp = base + st * L::kStage;
           uint8_t* a_hi = sp;
@@ -563,24 +586,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
               const int matom = wt / kVq;
               const int kv = (wt % kVq) * 4 + kq;
               const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
-              gen_octet<false>(sv[kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA);
+              gen_octet<false>(sv[kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA, fast);
             } else {
               const int w2 = wt - kTasksA;
               const int matom = w2 / kVq;
               const int kv = (w2 % kVq) * 4 + kq;
               const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
-              gen_octet<true>(sv[kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB);
+              gen_octet<true>(sv[kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB, fast);
             }
           }
           fence_proxy_async();
-          mbar_arrive(&op_full[st]);
-          mbar_arrive(&vis_empty[slot]);
+          warp_arrive(&op_full[st]);
+          warp_arrive(&vis_empty[slot]);
           const bool last = (n == nchunks - 1);
           const bool drain = last || ((n % kSlab) == kSlab - 1);
           const uint32_t my = nch;
           nch++;
           if (!drain) continue;
-          ok = mbar_wait(&op_empty[my & 1], (my >> 1) & 1, abort, p.err, 3u);
+          ok = warp_wait(&op_empty[my & 1], (my >> 1) & 1, abort, p.err, 3u);
           if (!ok) break;
           fence_after();
           // running sum += accumulator (short FP32 chains)
@@ -598,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           }
           run_empty = false;
           fence_before();
-          mbar_arrive(drained);
+          warp_arrive(drained);
           if (last) {
             // channel epilogue: partial (+)= factor * running sum
 #pragma unroll 1
@@ -679,6 +702,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
   p.normalize = P.normalize;
   p.flag_opt = flag_opt;
   p.mode = mode;
+  p.fast_anchor = P.tc_fast_anchor;
   const int TN = tc_tile_n(P);
   p.ntile_i = P.N / tc::kTM;
   p.ntile_j = P.N / TN;

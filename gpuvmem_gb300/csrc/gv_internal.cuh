@@ -121,6 +121,7 @@ struct Problem {
   uint32_t* d_flags = nullptr;   // [kNumFlags]
   float* tc_partial = nullptr;   // [tc_nsplit][MN] split-K partial images
   int tc_nsplit = 0;
+  int tc_fast_anchor = 1;        // SFU anchor phasor (GV_TC_ACCURATE_ANCHOR=1 selects sincospif)
   int num_sms = 0;
 };
 

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "gv_internal.cuh"
@@ -526,6 +527,8 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
       }
     }
     P.tc_nsplit = best;
+    const char* acc = std::getenv("GV_TC_ACCURATE_ANCHOR");
+    P.tc_fast_anchor = (acc && acc[0] == '1') ? 0 : 1;
     GV_CUDA(cudaMalloc(&P.tc_partial, sizeof(float) * (size_t)best * MN));
   }
   P.part_stride = 4 * P.num_sms;
