@@ -41,7 +41,9 @@
 // the kernel returns; the host turns the word into GV_ERR_DEVICE.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 
 #include "gv_internal.cuh"
 
@@ -57,7 +59,7 @@ constexpr int kGenThreads = kGenWarps * 32;
 constexpr int kThreads = kGenThreads + 32;
 constexpr int kVisSlots = 4;
 constexpr int kLookahead = kVisSlots - 1;
-constexpr int kSlab = 16;           // chunks accumulated before a drain
+constexpr int kSlab = 4;            // default chunks accumulated before a drain
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -65,7 +67,9 @@ struct VisEntry {
   uint32_t FU, FV;
   float GU, GV;
   float2 Eu, Ev;
-  float2 c;  // conj(w Vr) * scale
+  float2 c;      // conj(w Vr) * global scale / chunk scale
+  float ascale;  // chunk scale 2^e (e <= 0) applied to the A operand
+  float pad;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -235,6 +239,7 @@ struct TcParams {
   double DELTAX, DELTAY;
   int normalize, flag_opt, mode;
   int fast_anchor;  // 1: anchor phasor from the SFU (__sincosf), 0: sincospif
+  int slab;         // chunks accumulated in TMEM by the tensor core before a drain
   int ntile_i, ntile_j, nsplit;
   int C;
   int64_t Ktot;               // kept visibilities over all channels
@@ -306,7 +311,10 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
   else
     sincospif(2.0f * th, &sn, &cs);
   float2 v = make_float2(cs, sn);
-  if (kIsB) v = cmul(v, ve.c);
+  if (kIsB)
+    v = cmul(v, ve.c);
+  else
+    v = make_float2(v.x * ve.ascale, v.y * ve.ascale);
   // d = e^{2 pi i (f - G (2 r0 + 1))}, q = e^{-4 pi i G}; the chirp angles
   // are below 1e-3 rad, so second-order expansions are exact in FP32
   const float eps = -6.283185307179586f * G * (2.0f * rf + 1.0f);
@@ -484,6 +492,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         ve.Eu = ve.Ev = make_float2(1.0f, 0.0f);
         ve.c = make_float2(0.0f, 0.0f);
       }
+      // chunk scale: B carries c / 2^e, A carries b * 2^e (powers of two,
+      // exact), so small residuals keep FP16's relative precision
+      float m = fmaxf(fabsf(ve.c.x), fabsf(ve.c.y));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      int ce = 0;
+      if (m > 0.0f) frexpf(m, &ce);
+      ce = ce < -24 ? -24 : (ce > 0 ? 0 : ce);
+      ve.ascale = ldexpf(1.0f, ce);
+      ve.c = make_float2(ldexpf(ve.c.x, -ce), ldexpf(ve.c.y, -ce));
+      ve.pad = 0.0f;
       s_vis[slot * kChunkVis + lane] = ve;
       mbar_arrive(&vis_full[slot]);
       return true;
@@ -502,8 +521,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         if (!ok) break;
       }
       const int st = nch & 1;
-      const bool fresh = (mm.n % kSlab) == 0;
-      const bool drain = (mm.n == mm.nchunks - 1) || ((mm.n % kSlab) == kSlab - 1);
+      const bool fresh = (mm.n % p.slab) == 0;
+      const bool drain = (mm.n == mm.nchunks - 1) || ((mm.n % p.slab) == p.slab - 1);
       if (lane == 0) {
         ok = mbar_wait(&op_full[st], (nch >> 1) & 1, abort, p.err, 5u);
         if (ok && fresh && nch > 0) ok = mbar_wait(drained, (ndrain - 1) & 1, abort, p.err, 6u);
@@ -599,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           warp_arrive(&op_full[st]);
           warp_arrive(&vis_empty[slot]);
           const bool last = (n == nchunks - 1);
-          const bool drain = last || ((n % kSlab) == kSlab - 1);
+          const bool drain = last || ((n % p.slab) == p.slab - 1);
           const uint32_t my = nch;
           nch++;
           if (!drain) continue;
@@ -703,6 +722,10 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
   p.flag_opt = flag_opt;
   p.mode = mode;
   p.fast_anchor = P.tc_fast_anchor;
+  {
+    const char* sl = std::getenv("GV_TC_SLAB");
+    p.slab = sl ? std::max(1, std::atoi(sl)) : tc::kSlab;
+  }
   const int TN = tc_tile_n(P);
   p.ntile_i = P.N / tc::kTM;
   p.ntile_j = P.N / TN;

@@ -1,0 +1,2 @@
+/* empty stand-in: the reference harness compiles kernels only */
+#pragma once
