@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--config", type=int, default=1, choices=[0, 1])
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--case", default=None, help="run a profiling case instead of the bench")
     return ap.parse_args()
 
 
@@ -315,8 +316,37 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_case(name, reps):
+    """Small fixed workloads for profiling one kernel (used by the commands
+    recorded in profiles/): `dchi2_2048_1ch` (configuration 1 reduced to one
+    channel at 230 GHz, natural weights, 16 s integrations) and `cfg0`."""
+    import dataclasses
+    import torch
+    import gpuvmem_gb300 as gv
+    if name == "dchi2_2048_1ch":
+        cfg = dataclasses.replace(synth.CONFIG1, freqs_hz=[230e9], weighting="natural", dt_s=16.0)
+    elif name == "cfg0":
+        cfg = synth.CONFIG0
+    else:
+        raise SystemExit(f"unknown case {name}")
+    data = synth.generate(cfg, device="cuda")
+    prob = gv.Problem(data, [gv.term("Chi2", 1.0), gv.term("Entropy", 0.01)])
+    img = prob.initial_image()
+    prob.chi2(img)
+    xi = torch.zeros_like(img)
+    for _ in range(reps):
+        prob.objective(img)
+        prob.dchi2(img, out=xi)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "visibilities": int(data.nvis), "reps": reps,
+                      "engine": prob.info.dchi2_engine}))
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case, args.steps)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
