@@ -203,6 +203,24 @@ gv_status gv_dirty_image(gv_problem* p, float* d_out);
  * caller's visibility order, to a host buffer of 2*nvis_total floats. */
 gv_status gv_residuals(gv_problem* p, float* h_out);
 
+/* Prior value without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- code inside a host
+ * framework that owns all device memory, or a real-time loop where an
+ * allocation could synchronise the device.  Every input and output comes
+ * from the caller: d_plane is one N x N image plane (row-major), d_noise the
+ * N x N noise image (a pixel counts when noise < noise_cut, as the
+ * reference's mask), d_value one device double receiving the sum of the
+ * prior's per-pixel values (before lambda).  kind is GV_FI_ENTROPY ..
+ * GV_FI_LAPLACIAN; prior_value/eta/epsilon as gv_fi_desc.  The only scratch
+ * is a library-owned static device array of one FP64 partial per row, so
+ * n is limited to 8192 (GV_ERR_UNSUPPORTED beyond).  The first call on a
+ * device looks up that array's address; make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race.  Work is
+ * enqueued on `stream` (cudaStream_t, NULL = legacy default stream). */
+gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float* d_noise,
+                                float noise_cut, int32_t n, float prior_value, float eta,
+                                float epsilon, double* d_value, void* stream);
+
 const char* gv_last_error(void);
 const char* gv_version(void);
 /* Diagnostics (no counterpart in the reference): number of kernels the
