@@ -12,33 +12,42 @@
 // i.e. a real GEMM D = A B with K = 2V:  A[i][2k] = Re b, A[i][2k+1] = Im b,
 // B[2k][j] = Re x, B[2k+1][j] = -Im x.
 //
-// Operands are never materialised in HBM.  Per chunk of 32 visibilities,
-// 16 generator warps build the 128 x 64 A tile and the TN x 64 B tile in
-// shared memory: each thread produces 8 consecutive rows for one
-// visibility from an exact fixed-point anchor (the linear phase is reduced
-// mod 1 with 32-bit integer products) and a chirp recurrence in FP32.  Each
-// operand is split into FP16 hi + lo parts and the tile is accumulated with
-// three MMAs (hi*hi + hi*lo + lo*hi) into an FP32 accumulator in TMEM.
-// Operand tiles are MN-major with the 128-byte swizzle.
+// Operands are never materialised in HBM.  Per chunk of 32 visibilities the
+// generator warps build the 128 x 64 A tile and the TN x 64 B tile in shared
+// memory: each thread produces 8 consecutive rows for one visibility from an
+// exact fixed-point anchor (the linear phase is reduced mod 1 with 32-bit
+// integer products) and a chirp recurrence in FP32.  Each operand is split
+// into FP16 hi + lo parts and the tile is accumulated with three MMAs
+// (hi*hi + hi*lo + lo*hi) into an FP32 accumulator in TMEM.  Operand tiles are
+// MN-major with the 128-byte swizzle.
+//
+// Thread-block clusters of CS CTAs (CS = 1, 2 or 4) work on CS consecutive
+// row tiles of the same column tile and visibility range, so they need the
+// same B tile: each CTA generates 1/CS of B and writes it into the shared
+// memory of every CTA of its cluster (distributed shared memory); A stays
+// local.  Each CTA runs its own cta_group::1 MMAs on its own TMEM.  An MMA
+// commit is multicast to every CTA's "stage empty" barrier, since every
+// CTA writes into every stage.
 //
 // Warp roles (no block-wide barrier per chunk):
-//   warps 0..15  generators: wait for the chunk's visibility constants and
-//                a free operand stage, generate, arrive on the stage's
-//                "full" barrier; every kSlab chunks (and at the end of a
-//                channel) they drain the accumulator into a running sum in
-//                the other half of TMEM, and at the end of a channel apply
-//                the channel's epilogue factor (beam, fg_scale, chain rule)
-//                and add it to this split's partial image;
-//   warp 16      control: its lanes load the visibility constants of
-//                chunks up to three ahead into a 4-slot ring; its lane 0
-//                issues the MMAs of each full stage and commits them to the
-//                stage's "empty" barrier.
+//   generator warps  wait for the chunk's visibility constants and a stage
+//                    free in all CTAs of the cluster, generate, arrive on the
+//                    "stage full" barrier of every CTA; warps 0..7 also drain
+//                    the accumulator every `slab` chunks into a running sum
+//                    in the other half of TMEM, and at the end of a channel
+//                    apply the epilogue factor (beam, fg_scale, chain rule)
+//                    and add it to this split's partial image;
+//   control warp     its lanes load the visibility constants of chunks up to
+//                    three ahead into a 4-slot ring; its lane 0 issues the
+//                    MMAs of each full stage and commits them.
 // Split-K partials are summed in FP64 in a fixed order, so results are
 // deterministic.
 //
 // Every wait is bounded: on timeout the kernel records an error word, every
-// warp stops, the MMAs in flight are waited for (bounded), TMEM is freed and
-// the kernel returns; the host turns the word into GV_ERR_DEVICE.
+// warp stops, the MMAs in flight are waited for (bounded), the cluster
+// meets at a final barrier so no CTA exits while a peer may still write into
+// its shared memory, TMEM is freed and the kernel returns; the host turns
+// the word into GV_ERR_DEVICE.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -54,14 +63,23 @@ namespace tc {
 constexpr int kTM = 128;            // image rows per tile (MMA M)
 constexpr int kChunkVis = 32;       // visibilities per chunk
 constexpr int kKC = 2 * kChunkVis;  // K elements per chunk
-constexpr int kGenWarps = 16;
-constexpr int kGenThreads = kGenWarps * 32;
-constexpr int kThreads = kGenThreads + 32;
+constexpr int kDrainWarps = 8;      // warps that drain TMEM (4 lane quarters x 2 halves)
 constexpr int kVisSlots = 4;
 constexpr int kLookahead = kVisSlots - 1;
 constexpr int kSlab = 4;            // default chunks accumulated before a drain
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+// generator warps per CTA: every warp gets the same number of warp-tasks per
+// chunk.  A warp-task is 64 rows x 4*vpl visibilities (vpl = visibilities
+// per lane, generated as independent instruction streams for ILP); for
+// TN = 256 a chunk has 16/vpl A tasks and 32/(cs*vpl) B tasks.
+__host__ __device__ constexpr int gen_warps(int cs, int vpl) {
+  return vpl == 2 ? 12 : (cs == 4 ? 12 : 16);
+}
+__host__ __device__ constexpr int threads_for(int cs, int vpl) {
+  return gen_warps(cs, vpl) * 32 + 32;
+}
 
 struct VisEntry {
   uint32_t FU, FV;
@@ -80,18 +98,53 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// ---- tcgen05 / mbarrier wrappers (inline PTX) -------------------------------
+// ---- cluster / tcgen05 / mbarrier wrappers (inline PTX) ---------------------
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t num_clusters() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+// shared::cluster address of `local` in CTA `rank` of this cluster
+__device__ __forceinline__ uint32_t map_rank(uint32_t local, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint4 v) {
+  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
 __device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
 }
+// arrive, with release at cluster scope, on a barrier of any CTA of the cluster
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
+               : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
       : "r"(smem_u32(m)), "r"(parity)
@@ -147,8 +200,9 @@ __device__ __forceinline__ void fence_before() {
 __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
+// generic-proxy writes (local and remote shared memory) -> async proxy
 __device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("fence.proxy.async;" ::: "memory");
 }
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
                                         uint32_t idesc, uint32_t accum) {
@@ -163,6 +217,14 @@ __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(mbar))
+      : "memory");
+}
+// commit arriving on the barrier at the same offset in every CTA of `mask`
+__device__ __forceinline__ void mma_commit_multicast(uint64_t* mbar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(smem_u32(mbar)),
+      "h"(mask)
       : "memory");
 }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
@@ -291,11 +353,14 @@ __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int
   return 0.0f;
 }
 
-// Generate 8 consecutive rows of one operand for one visibility and store
-// the FP16 hi/lo parts of Re and (sign-adjusted) Im.
+struct Octet {
+  uint4 hre, him, lre, lim;
+};
+
+// 8 consecutive rows of one operand for one visibility: FP16 hi/lo parts of
+// Re and (sign-adjusted) Im, packed for 16-byte stores.
 template <bool kIsB>
-__device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* hi, uint8_t* lo,
-                                          int matom, int oct, int kv, uint32_t sbo, bool fast) {
+__device__ __forceinline__ Octet gen_octet(const VisEntry& ve, int r0, bool fast) {
   const uint32_t F = kIsB ? ve.FU : ve.FV;
   const float G = kIsB ? ve.GU : ve.GV;
   const float2 E = kIsB ? ve.Eu : ve.Ev;
@@ -344,17 +409,17 @@ __device__ __forceinline__ void gen_octet(const VisEntry& ve, int r0, uint8_t* h
     lre[t] = *reinterpret_cast<const uint32_t*>(&l_re);
     lim[t] = *reinterpret_cast<const uint32_t*>(&l_im);
   }
-  const uint32_t ore = tile_off(matom, oct, 2 * kv, sbo);
-  const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, sbo);
-  *reinterpret_cast<uint4*>(hi + ore) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-  *reinterpret_cast<uint4*>(hi + oim) = make_uint4(him[0], him[1], him[2], him[3]);
-  *reinterpret_cast<uint4*>(lo + ore) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-  *reinterpret_cast<uint4*>(lo + oim) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
+  Octet o;
+  o.hre = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+  o.him = make_uint4(him[0], him[1], him[2], him[3]);
+  o.lre = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+  o.lim = make_uint4(lim[0], lim[1], lim[2], lim[3]);
+  return o;
 }
 
-// The chunk sequence every warp walks in the same order: work items
-// (tile, split) owned by this CTA, the channels each split overlaps, and
-// 32-visibility chunks within a channel.
+// The chunk sequence every warp of every CTA of a cluster walks in the same
+// order: the cluster's work items (row-tile group, column tile, split), the
+// channels each split overlaps, and 32-visibility chunks within a channel.
 struct ChunkIter {
   int item, c, n, nchunks;
   int64_t goff, nvis;
@@ -369,8 +434,8 @@ __device__ __forceinline__ void item_range(const TcParams& p, int item, int64_t*
 }
 
 // position `it` on the first chunk at or after (item, channel c); returns
-// false when the CTA has no more chunks
-__device__ bool iter_seek(const TcParams& p, int nitems, ChunkIter& it) {
+// false when the cluster has no more chunks
+__device__ bool iter_seek(const TcParams& p, int nitems, int stride, ChunkIter& it) {
   while (it.item < nitems) {
     int64_t ks, ke;
     item_range(p, it.item, &ks, &ke);
@@ -386,56 +451,64 @@ __device__ bool iter_seek(const TcParams& p, int nitems, ChunkIter& it) {
         return true;
       }
     }
-    it.item += gridDim.x;
+    it.item += stride;
     it.c = 0;
   }
   it.valid = false;
   return false;
 }
 
-__device__ __forceinline__ void iter_next(const TcParams& p, int nitems, ChunkIter& it) {
+__device__ __forceinline__ void iter_next(const TcParams& p, int nitems, int stride,
+                                          ChunkIter& it) {
   if (++it.n < it.nchunks) return;
   it.c++;
-  iter_seek(p, nitems, it);
+  iter_seek(p, nitems, stride, it);
 }
 
-template <int TN>
-__global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
+template <int TN, int CS, int VPL>
+__global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p) {
   using L = Layout<TN>;
+  constexpr int GW = gen_warps(CS, VPL);
+  constexpr int kMB = TN / 64;        // MN atoms of B
+  constexpr int kMBown = kMB / CS;    // B atoms this CTA generates
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
   VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + 2 * L::kStage);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
-  uint64_t* op_full = bars;                  // [2]  one arrive per generator warp
-  uint64_t* op_empty = bars + 2;             // [2]  tcgen05.commit
-  uint64_t* vis_full = bars + 4;             // [4]  count 32 (control lanes)
-  uint64_t* vis_empty = bars + 8;            // [4]  one arrive per generator warp
-  uint64_t* drained = bars + 12;             // [1]  one arrive per generator warp
+  uint64_t* op_full = bars;       // [2]  one arrive per generator warp per CTA of the cluster
+  uint64_t* op_empty = bars + 2;  // [2]  one MMA commit per CTA of the cluster
+  uint64_t* vis_full = bars + 4;  // [4]  32 arrives (control lanes)
+  uint64_t* vis_empty = bars + 8; // [4]  one arrive per generator warp
+  uint64_t* drained = bars + 12;  // [1]  one arrive per draining warp
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 16);
   __shared__ int s_abort;
   volatile int* abort = &s_abort;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = CS > 1 ? cluster_rank() : 0u;
+  const int cid = CS > 1 ? (int)cluster_id() : (int)blockIdx.x;
+  const int ncl = CS > 1 ? (int)num_clusters() : (int)gridDim.x;
   if (warp == 0) {
     tmem_alloc(tslot, kTmemCols);
     tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(&op_full[0], kGenWarps);
-    mbar_init(&op_full[1], kGenWarps);
-    mbar_init(&op_empty[0], 1);
-    mbar_init(&op_empty[1], 1);
+    mbar_init(&op_full[0], GW * CS);
+    mbar_init(&op_full[1], GW * CS);
+    mbar_init(&op_empty[0], CS);
+    mbar_init(&op_empty[1], CS);
     for (int s = 0; s < kVisSlots; s++) {
       mbar_init(&vis_full[s], 32);
-      mbar_init(&vis_empty[s], kGenWarps);
+      mbar_init(&vis_empty[s], GW);
     }
-    mbar_init(drained, kGenWarps);
+    mbar_init(drained, kDrainWarps);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   fence_before();
   __syncthreads();
+  if (CS > 1) cluster_sync();  // peers' barriers are initialised before any remote access
   fence_after();
   const uint32_t tbase = *tslot;
   const uint32_t t_acc = tbase;
@@ -447,15 +520,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   if (cmax > 0.0f) frexpf(cmax, &e);
   const float scale = ldexpf(1.0f, -e);
   const float inv_s = ldexpf(1.0f, e);
-  const int nitems = p.ntile_i * p.ntile_j * p.nsplit;
-  uint32_t nch = 0;  // position in this CTA's chunk sequence
+  const int nitems = (p.ntile_i / CS) * p.ntile_j * p.nsplit;
+  uint32_t nch = 0;  // position in the cluster's chunk sequence
 
-  if (warp == kGenWarps) {
+  if (warp == GW) {
     // ------------------------------- control warp --------------------------
-    ChunkIter ld{(int)blockIdx.x, 0, 0, 0, 0, 0, false};
+    ChunkIter ld{cid, 0, 0, 0, 0, 0, false};
     ChunkIter mm = ld;
-    iter_seek(p, nitems, ld);
-    iter_seek(p, nitems, mm);
+    iter_seek(p, nitems, ncl, ld);
+    iter_seek(p, nitems, ncl, mm);
     uint32_t nld = 0, ndrain = 0;
     const uint32_t idesc = make_idesc(kTM, TN);
     bool ok = true;
@@ -511,13 +584,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
     while (ok && ld.valid && nld < (uint32_t)kLookahead) {
       ok = load_one(ld, nld);
       nld++;
-      iter_next(p, nitems, ld);
+      iter_next(p, nitems, ncl, ld);
     }
     while (ok && mm.valid) {
       if (ld.valid) {
         ok = load_one(ld, nld);
         nld++;
-        iter_next(p, nitems, ld);
+        iter_next(p, nitems, ncl, ld);
         if (!ok) break;
       }
       const int st = nch & 1;
@@ -541,15 +614,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
             mma_f16(t_acc, ah, bl, idesc, 1u);
             mma_f16(t_acc, al, bh, idesc, 1u);
           }
-          mma_commit(&op_empty[st]);
+          if (CS > 1)
+            mma_commit_multicast(&op_empty[st], (uint16_t)((1u << CS) - 1u));
+          else
+            mma_commit(&op_empty[st]);
         }
       }
       ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       if (drain) ndrain++;
       nch++;
-      iter_next(p, nitems, mm);
+      iter_next(p, nitems, ncl, mm);
     }
-    // retire: no MMA may be in flight when TMEM is freed
+    // retire: no MMA of this CTA may be in flight when TMEM is freed (the
+    // barrier also counts the peers' commits, which only makes this later)
     if (lane == 0 && nch > 0) {
       const uint32_t q = nch - 1;
       const long long t0 = clock64();
@@ -564,23 +641,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
     // ----------------------------- generator warps -------------------------
     const int oct = lane & 7, kq = lane >> 3;
     const bool fast = p.fast_anchor != 0;
-    constexpr int kVq = kChunkVis / 4;  // visibility quads per chunk
+    constexpr int kVq = kChunkVis / (4 * VPL);  // visibility groups per chunk
     constexpr int kTasksA = (kTM / 64) * kVq;
-    constexpr int kTasksB = (TN / 64) * kVq;
-    constexpr int kCols = TN / 4;       // epilogue columns per thread
-    const int lq = warp & 3, cg = warp >> 2;
+    constexpr int kTasksB = kMBown * kVq;
+    constexpr int kCols = TN / 2;             // epilogue columns per draining thread
+    const bool drainer = warp < kDrainWarps;
+    const int lq = warp & 3, half = (warp >> 2) & 1;
     const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
+    // shared::cluster addresses of both stages' B tiles and op_full barriers
+    // in every CTA of the cluster
+    uint32_t bhi_r[2][CS], blo_r[2][CS], full_r[2][CS];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const uint32_t lb = smem_u32(base + s * L::kStage + 2 * L::kTileA);
+#pragma unroll
+      for (int r = 0; r < CS; r++) {
+        bhi_r[s][r] = CS > 1 ? map_rank(lb, r) : lb;
+        blo_r[s][r] = CS > 1 ? map_rank(lb + L::kTileB, r) : lb + L::kTileB;
+        full_r[s][r] = CS > 1 ? map_rank(smem_u32(&op_full[s]), r) : smem_u32(&op_full[s]);
+      }
+    }
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    for (int item = cid; item < nitems && ok; item += ncl) {
       const int split = item % p.nsplit;
       const int tile = item / p.nsplit;
-      const int ti = tile / p.ntile_j, tj = tile % p.ntile_j;
-      const int i0 = ti * kTM, j0 = tj * TN;
+      const int tig = tile / p.ntile_j, tj = tile % p.ntile_j;
+      const int i0 = (tig * CS + (int)rank) * kTM, j0 = tj * TN;
       int64_t ks, ke;
       item_range(p, item, &ks, &ke);
       bool first_channel = true;
       const int ei = i0 + 32 * lq + lane;
-      const int ej0 = j0 + cg * kCols;
+      const int ej0 = j0 + half * kCols;
       float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + ej0;
       for (int c = 0; c < p.C && ok; c++) {
         const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
@@ -597,38 +688,76 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           uint8_t* sp = base + st * L::kStage;
           uint8_t* a_hi = sp;
           uint8_t* a_lo = sp + L::kTileA;
-          uint8_t* b_hi = sp + 2 * L::kTileA;
-          uint8_t* b_lo = sp + 2 * L::kTileA + L::kTileB;
           const VisEntry* sv = s_vis + slot * kChunkVis;
-          for (int wt = warp; wt < kTasksA + kTasksB; wt += kGenWarps) {
+          for (int wt = warp; wt < kTasksA + kTasksB; wt += GW) {
             if (wt < kTasksA) {
               const int matom = wt / kVq;
-              const int kv = (wt % kVq) * 4 + kq;
+              const int kv0 = (wt % kVq) * 4 * VPL + kq;
               const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
-              gen_octet<false>(sv[kv], r0, a_hi, a_lo, matom, oct, kv, L::kSboA, fast);
+              Octet o[VPL];
+#pragma unroll
+              for (int v = 0; v < VPL; v++) o[v] = gen_octet<false>(sv[kv0 + 4 * v], r0, fast);
+#pragma unroll
+              for (int v = 0; v < VPL; v++) {
+                const int kv = kv0 + 4 * v;
+                const uint32_t ore = tile_off(matom, oct, 2 * kv, L::kSboA);
+                const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, L::kSboA);
+                *reinterpret_cast<uint4*>(a_hi + ore) = o[v].hre;
+                *reinterpret_cast<uint4*>(a_hi + oim) = o[v].him;
+                *reinterpret_cast<uint4*>(a_lo + ore) = o[v].lre;
+                *reinterpret_cast<uint4*>(a_lo + oim) = o[v].lim;
+              }
             } else {
               const int w2 = wt - kTasksA;
-              const int matom = w2 / kVq;
-              const int kv = (w2 % kVq) * 4 + kq;
+              const int matom = (int)rank * kMBown + w2 / kVq;
+              const int kv0 = (w2 % kVq) * 4 * VPL + kq;
               const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
-              gen_octet<true>(sv[kv], r0, b_hi, b_lo, matom, oct, kv, L::kSboB, fast);
+              Octet o[VPL];
+#pragma unroll
+              for (int v = 0; v < VPL; v++) o[v] = gen_octet<true>(sv[kv0 + 4 * v], r0, fast);
+#pragma unroll
+              for (int v = 0; v < VPL; v++) {
+                const int kv = kv0 + 4 * v;
+                const uint32_t ore = tile_off(matom, oct, 2 * kv, L::kSboB);
+                const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, L::kSboB);
+                if (CS == 1) {
+                  uint8_t* b_hi = sp + 2 * L::kTileA;
+                  uint8_t* b_lo = b_hi + L::kTileB;
+                  *reinterpret_cast<uint4*>(b_hi + ore) = o[v].hre;
+                  *reinterpret_cast<uint4*>(b_hi + oim) = o[v].him;
+                  *reinterpret_cast<uint4*>(b_lo + ore) = o[v].lre;
+                  *reinterpret_cast<uint4*>(b_lo + oim) = o[v].lim;
+                } else {
+#pragma unroll
+                  for (int r = 0; r < CS; r++) {
+                    st_cluster_v4(bhi_r[st][r] + ore, o[v].hre);
+                    st_cluster_v4(bhi_r[st][r] + oim, o[v].him);
+                    st_cluster_v4(blo_r[st][r] + ore, o[v].lre);
+                    st_cluster_v4(blo_r[st][r] + oim, o[v].lim);
+                  }
+                }
+              }
             }
           }
           fence_proxy_async();
-          warp_arrive(&op_full[st]);
+          __syncwarp();
+          if (lane == 0) {
+#pragma unroll
+            for (int r = 0; r < CS; r++) mbar_arrive_cluster(full_r[st][r]);
+          }
           warp_arrive(&vis_empty[slot]);
           const bool last = (n == nchunks - 1);
           const bool drain = last || ((n % p.slab) == p.slab - 1);
           const uint32_t my = nch;
           nch++;
-          if (!drain) continue;
+          if (!drain || !drainer) continue;
           ok = warp_wait(&op_empty[my & 1], (my >> 1) & 1, abort, p.err, 3u);
           if (!ok) break;
           fence_after();
           // running sum += accumulator (short FP32 chains)
 #pragma unroll 1
           for (int cb = 0; cb < kCols; cb += 32) {
-            const uint32_t col = (uint32_t)(cg * kCols + cb);
+            const uint32_t col = (uint32_t)(half * kCols + cb);
             float acc[32], run[32];
             tmem_ld32(t_acc + lane_off + col, acc);
             if (!run_empty) {
@@ -645,7 +774,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
             // channel epilogue: partial (+)= factor * running sum
 #pragma unroll 1
             for (int cb = 0; cb < kCols; cb += 32) {
-              const uint32_t col = (uint32_t)(cg * kCols + cb);
+              const uint32_t col = (uint32_t)(half * kCols + cb);
               float run[32];
               tmem_ld32(t_run + lane_off + col, run);
 #pragma unroll 4
@@ -662,7 +791,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           }
         }
       }
-      if (ok && first_channel) {
+      if (ok && first_channel && drainer) {
         // no visibilities in this split for this tile: its partial is zero
         for (int k = 0; k < kCols; k++) prow[k] = 0.0f;
       }
@@ -670,6 +799,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   }
   fence_before();
   __syncthreads();
+  if (CS > 1) cluster_sync();  // no CTA leaves while a peer may still write into it
   fence_after();
   if (warp == 0) tmem_dealloc(tbase, kTmemCols);
 }
@@ -684,6 +814,40 @@ __global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restric
   out[q] += (float)s;
 }
 
+template <int TN, int CS, int VPL>
+gv_status launch_tc(const Problem& P, const TcParams& p, int nitems) {
+  auto kern = k_dchi2_tc<TN, CS, VPL>;
+  const size_t smem = Layout<TN>::kSmem;
+  GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  cfg.blockDim = dim3(threads_for(CS, VPL), 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = P.stream;
+  int nclusters = P.num_sms / CS;
+  if (CS > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(CS * nclusters, 1, 1);
+    int active = 0;
+    GV_CUDA(cudaOccupancyMaxActiveClusters(&active, kern, &cfg));
+    if (active <= 0) {
+      set_error("no cluster of the tensor-core DChi2 kernel fits on this device");
+      return GV_ERR_UNSUPPORTED;
+    }
+    nclusters = std::min(nclusters, active);
+  }
+  nclusters = std::max(1, std::min(nclusters, nitems));
+  cfg.gridDim = dim3(CS * nclusters, 1, 1);
+  GV_CUDA(cudaLaunchKernelEx(&cfg, kern, p));
+  GV_LAUNCH("k_dchi2_tc");
+  return GV_OK;
+}
+
 }  // namespace tc
 
 bool dchi2_tc_supported(const Problem& P) {
@@ -692,8 +856,18 @@ bool dchi2_tc_supported(const Problem& P) {
 
 int tc_tile_n(const Problem& P) { return P.N >= 256 ? 256 : 128; }
 
-size_t tc_smem_bytes(int tn) {
-  return tn == 256 ? tc::Layout<256>::kSmem : tc::Layout<128>::kSmem;
+// cluster size: the largest of 4, 2, 1 dividing the row tiles and the B atoms
+int tc_cluster(const Problem& P) {
+  const int TN = tc_tile_n(P);
+  const int ntile_i = P.N / tc::kTM;
+  // measured on GB300 (2048^2, 35.28M visibilities): 1 CTA 2.30 s, clusters
+  // of 2 3.44 s, of 4 5.48 s -- the remote 16-byte stores of the shared B
+  // tile cost more than the generation they save -- so clusters are opt-in
+  int cs = 1;
+  const char* env = std::getenv("GV_TC_CLUSTER");
+  if (env) cs = std::atoi(env);
+  while (cs > 1 && (ntile_i % cs != 0 || (TN / 64) % cs != 0 || (cs != 2 && cs != 4))) cs /= 2;
+  return cs < 1 ? 1 : cs;
 }
 
 gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result,
@@ -727,6 +901,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.slab = sl ? std::max(1, std::atoi(sl)) : tc::kSlab;
   }
   const int TN = tc_tile_n(P);
+  const int CS = tc_cluster(P);
   p.ntile_i = P.N / tc::kTM;
   p.ntile_j = P.N / TN;
   p.nsplit = P.tc_nsplit;
@@ -755,19 +930,22 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.kc_off = P.d_kc_off;
     p.Ktot = P.Vgrid;
   }
-  const int nitems = p.ntile_i * p.ntile_j * p.nsplit;
-  const int grid = nitems < P.num_sms ? nitems : P.num_sms;
-  const size_t smem = tc_smem_bytes(TN);
+  const int nitems = (p.ntile_i / CS) * p.ntile_j * p.nsplit;
+  // visibilities per generator lane (independent chains for ILP)
+  int vpl = 2;
+  if (const char* v = std::getenv("GV_TC_VPL")) vpl = std::atoi(v) == 1 ? 1 : 2;
+  gv_status s;
   if (TN == 256) {
-    GV_CUDA(cudaFuncSetAttribute(tc::k_dchi2_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    tc::k_dchi2_tc<256><<<grid, tc::kThreads, smem, P.stream>>>(p);
+    if (CS == 4) s = tc::launch_tc<256, 4, 1>(P, p, nitems);
+    else if (CS == 2) s = tc::launch_tc<256, 2, 1>(P, p, nitems);
+    else if (vpl == 2) s = tc::launch_tc<256, 1, 2>(P, p, nitems);
+    else s = tc::launch_tc<256, 1, 1>(P, p, nitems);
   } else {
-    GV_CUDA(cudaFuncSetAttribute(tc::k_dchi2_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    tc::k_dchi2_tc<128><<<grid, tc::kThreads, smem, P.stream>>>(p);
+    if (CS == 2) s = tc::launch_tc<128, 2, 1>(P, p, nitems);
+    else if (vpl == 2) s = tc::launch_tc<128, 1, 2>(P, p, nitems);
+    else s = tc::launch_tc<128, 1, 1>(P, p, nitems);
   }
-  GV_LAUNCH("k_dchi2_tc");
+  if (s != GV_OK) return s;
   float* out = d_result + (mode == 0 ? (int64_t)(flag_opt % 2) * p.MN : 0);
   tc::k_reduce_partials<<<(unsigned)((p.MN + 255) / 256), 256, 0, P.stream>>>(
       p.MN, p.nsplit, P.tc_partial, out);
