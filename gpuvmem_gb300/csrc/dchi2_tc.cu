@@ -13,46 +13,57 @@
 // B[2k][j] = Re x, B[2k+1][j] = -Im x.
 //
 // Operands are never materialised in HBM.  Per chunk of 32 visibilities the
-// generator warps build the 128 x 64 A tile and the TN x 64 B tile in shared
-// memory: each thread produces 8 consecutive rows for one visibility from an
-// exact fixed-point anchor (the linear phase is reduced mod 1 with 32-bit
-// integer products) and a chirp recurrence in FP32.  Each operand is split
-// into FP16 hi + lo parts and the tile is accumulated with three MMAs
-// (hi*hi + hi*lo + lo*hi) into an FP32 accumulator in TMEM.  Operand tiles are
-// MN-major with the 128-byte swizzle.
+// generator warps build the A and B tiles in shared memory: each lane
+// produces 8 consecutive rows for two visibilities from an exact fixed-point
+// anchor (the linear phase is reduced mod 1 with 32-bit integer products)
+// and a chirp recurrence in FP32.  Each operand is split into FP16 hi + lo
+// parts and the tile is accumulated with three MMAs (hi*hi + hi*lo + lo*hi)
+// into an FP32 accumulator in TMEM.  Operand tiles are MN-major with the
+// 128-byte swizzle.
 //
-// Thread-block clusters of CS CTAs (CS = 1, 2 or 4) work on CS consecutive
-// row tiles of the same column tile and visibility range, so they need the
-// same B tile: each CTA generates 1/CS of B and writes it into the shared
-// memory of every CTA of its cluster (distributed shared memory); A stays
-// local.  Each CTA runs its own cta_group::1 MMAs on its own TMEM.  An MMA
-// commit is multicast to every CTA's "stage empty" barrier, since every
-// CTA writes into every stage.
+// Pair mode (image side >= 256): a cluster of two CTAs on one TPC runs
+// cta_group::2 MMAs with M = 256.  Each CTA holds 128 image rows of A and
+// half of the 256 columns of B, and receives its 128 x 256 block of the
+// product in its own TMEM, so per output pixel each SM generates 2/3 of the
+// operand rows a single-CTA 128 x 256 tile needs.  Single mode (image side
+// 128, or GV_TC_PAIR=0) runs cta_group::1 MMAs with M = 128.
+//
+// The accumulator is issued as two halves of TN/2 columns.  Every `slab`
+// chunks it is drained into a running sum in the other half of TMEM; the
+// first half is drained while the tensor core still works on the second,
+// and the next slab's first MMAs wait only for the first half, so the
+// tensor pipe does not stall on drains.
 //
 // Warp roles (no block-wide barrier per chunk):
-//   generator warps  wait for the chunk's visibility constants and a stage
-//                    free in all CTAs of the cluster, generate, arrive on the
-//                    "stage full" barrier of every CTA; warps 0..7 also drain
-//                    the accumulator every `slab` chunks into a running sum
-//                    in the other half of TMEM, and at the end of a channel
-//                    apply the epilogue factor (beam, fg_scale, chain rule)
-//                    and add it to this split's partial image;
-//   control warp     its lanes load the visibility constants of chunks up to
-//                    three ahead into a 4-slot ring; its lane 0 issues the
-//                    MMAs of each full stage and commits them.
+//   8 generator warps   wait for the chunk's visibility constants and a free
+//                       stage, generate, and arrive on the stage's "full"
+//                       barrier;
+//   4 drain warps       (one per TMEM lane quarter) drain the accumulator
+//                       halves into the running sum, and at the end of a
+//                       channel apply the epilogue factor (beam, fg_scale,
+//                       chain rule) and add it to this split's partial image;
+//   loader warp         loads the visibility constants of chunks up to five
+//                       ahead into a 6-slot ring (global loads issued two
+//                       chunks before they are needed);
+//   MMA warp            in the leader CTA, lane 0 issues the MMAs of each
+//                       full stage and commits them to both CTAs' barriers;
+//                       in the peer CTA, lane 0 forwards the stage's
+//                       completion to the leader (one cluster-scope arrive
+//                       per chunk instead of one per generator warp).
 // Split-K partials are summed in FP64 in a fixed order, so results are
 // deterministic.
 //
 // Every wait is bounded: on timeout the kernel records an error word, every
-// warp stops, the MMAs in flight are waited for (bounded), the cluster
-// meets at a final barrier so no CTA exits while a peer may still write into
-// its shared memory, TMEM is freed and the kernel returns; the host turns
-// the word into GV_ERR_DEVICE.
+// warp of the CTA stops, the MMAs in flight are waited for (bounded), the
+// pair meets at a final cluster barrier so no CTA exits while its peer may
+// still read its shared memory or write its TMEM, TMEM is freed and the
+// kernel returns; the host turns the word into GV_ERR_DEVICE.
 #include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
+#include <type_traits>
 
 #include "gv_internal.cuh"
 
@@ -60,32 +71,25 @@ namespace gv {
 
 namespace tc {
 
-constexpr int kTM = 128;            // image rows per tile (MMA M)
+constexpr int kTM = 128;            // image rows per CTA tile (MMA M per CTA)
 constexpr int kChunkVis = 32;       // visibilities per chunk
 constexpr int kKC = 2 * kChunkVis;  // K elements per chunk
-constexpr int kDrainWarps = 8;      // warps that drain TMEM (4 lane quarters x 2 halves)
-constexpr int kVisSlots = 4;
-constexpr int kLookahead = kVisSlots - 1;
+constexpr int kGW = 8;              // generator warps (two per scheduler)
+constexpr int kDW = 4;              // drain warps (one per TMEM lane quarter)
+// generator, drain, loader and MMA warps: 14 warps, at most 4 per scheduler,
+// so up to 128 registers a thread
+constexpr int kThreads = (kGW + kDW + 2) * 32;
+constexpr int kVPL = 2;             // visibilities per generator lane (packed FP32x2 chains)
+constexpr int kVisSlots = 6;
 constexpr int kSlab = 4;            // default chunks accumulated before a drain
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
-
-// generator warps per CTA: every warp gets the same number of warp-tasks per
-// chunk.  A warp-task is 64 rows x 4*vpl visibilities (vpl = visibilities
-// per lane, generated as independent instruction streams for ILP); for
-// TN = 256 a chunk has 16/vpl A tasks and 32/(cs*vpl) B tasks.
-__host__ __device__ constexpr int gen_warps(int cs, int vpl) {
-  return vpl == 2 ? 12 : (cs == 4 ? 12 : 16);
-}
-__host__ __device__ constexpr int threads_for(int cs, int vpl) {
-  return gen_warps(cs, vpl) * 32 + 32;
-}
 
 struct VisEntry {
   uint32_t FU, FV;
   float GU, GV;
   float2 Eu, Ev;
-  float2 c;      // conj(w Vr) * global scale / chunk scale
+  float2 c;      // w Vr * global scale / chunk scale
   float ascale;  // chunk scale 2^e (e <= 0) applied to the A operand
   float pad;
 };
@@ -124,11 +128,6 @@ __device__ __forceinline__ uint32_t map_rank(uint32_t local, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint4 v) {
-  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
-               "r"(v.y), "r"(v.z), "r"(v.w)
-               : "memory");
-}
 __device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
 }
@@ -139,6 +138,15 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
                : "memory");
+}
+// arrive on the barrier at the same offset in the leader CTA (rank 0) of the
+// pair, or on the local one in single mode
+template <bool PAIR>
+__device__ __forceinline__ void arrive_leader(uint64_t* m) {
+  if (PAIR)
+    mbar_arrive_cluster(map_rank(smem_u32(m), 0u));
+  else
+    mbar_arrive(m);
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
   uint32_t ok;
@@ -151,20 +159,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// as above, but the thread may stay suspended in the barrier for up to
+// kSuspendNs (it resumes as soon as the phase completes), so waiting warps
+// do not take issue slots from the generator warps
+constexpr uint32_t kSuspendNs = 20000;
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* m, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
 // bounded wait; returns false on timeout or when another warp gave up
 __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, volatile int* abort,
                                           uint32_t* err, uint32_t code) {
   if (mbar_try_wait(m, parity)) return true;
   const long long t0 = clock64();
-  for (uint32_t it = 1;; it++) {
-    if (mbar_try_wait(m, parity)) return true;
-    if ((it & 15) == 0) {
-      if (*abort) return false;
-      if (clock64() - t0 > kWaitCycles) {
-        atomicExch(err, code);
-        *abort = 1;
-        return false;
-      }
+  for (;;) {
+    if (mbar_try_wait_sleep(m, parity)) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      atomicExch(err, code);
+      *abort = 1;
+      return false;
     }
   }
 }
@@ -181,18 +202,39 @@ __device__ __forceinline__ void warp_arrive(uint64_t* m) {
   __syncwarp();
   if ((threadIdx.x & 31) == 0) mbar_arrive(m);
 }
+template <bool PAIR>
+__device__ __forceinline__ void warp_arrive_leader(uint64_t* m) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) arrive_leader<PAIR>(m);
+}
+template <bool PAIR>
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                   smem_u32(slot)),
-               "r"(ncols)
-               : "memory");
+  if (PAIR)
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+  else
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
 }
+template <bool PAIR>
 __device__ __forceinline__ void tmem_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  if (PAIR)
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  else
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
+template <bool PAIR>
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
-               : "memory");
+  if (PAIR)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+  else
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
 }
 __device__ __forceinline__ void fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -200,32 +242,43 @@ __device__ __forceinline__ void fence_before() {
 __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// generic-proxy writes (local and remote shared memory) -> async proxy
+// generic-proxy shared-memory writes -> async proxy (the tensor core)
 __device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+template <bool PAIR>
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
                                         uint32_t idesc, uint32_t accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
-      : "memory");
+  if (PAIR)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
 }
+// commit the MMAs issued so far: one arrive on `mbar` when they complete, in
+// both CTAs of the pair (same barrier offset) or in this CTA
+template <bool PAIR>
 __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(mbar))
-      : "memory");
-}
-// commit arriving on the barrier at the same offset in every CTA of `mask`
-__device__ __forceinline__ void mma_commit_multicast(uint64_t* mbar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
-      "[%0], %1;" ::"r"(smem_u32(mbar)),
-      "h"(mask)
-      : "memory");
+  if (PAIR)
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+        "[%0], %1;" ::"r"(smem_u32(mbar)),
+        "h"((uint16_t)3)
+        : "memory");
+  else
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(mbar))
+        : "memory");
 }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   uint32_t r[32];
@@ -321,16 +374,23 @@ struct TcParams {
   uint32_t* err;
 };
 
-template <int TN>
+// Shared-memory layout of one CTA.  A: 128 rows; B: the TN columns of the
+// tile (single) or this CTA's TN/2 of them (pair).  B atom a of the CTA
+// belongs to accumulator half a / kHatoms.
+template <int TN, bool PAIR>
 struct Layout {
-  static constexpr uint32_t kSboA = (kTM / 64) * 1024;  // bytes between K atoms of A
-  static constexpr uint32_t kSboB = (TN / 64) * 1024;
+  static constexpr int kBcols = PAIR ? TN / 2 : TN;
+  static constexpr int kBatoms = kBcols / 64;
+  static constexpr int kHatoms = kBatoms / 2;            // B atoms per accumulator half
+  static constexpr uint32_t kSboA = (kTM / 64) * 1024;   // bytes between K atoms of A
+  static constexpr uint32_t kSboB = kBatoms * 1024;
   static constexpr uint32_t kTileA = kSboA * (kKC / 8);  // one A part (hi or lo)
   static constexpr uint32_t kTileB = kSboB * (kKC / 8);
   static constexpr uint32_t kStage = 2 * kTileA + 2 * kTileB;
+  static constexpr int kStages = kStage <= 65536 ? 3 : 2;
   static constexpr uint32_t kVis = kVisSlots * kChunkVis * sizeof(VisEntry);
-  static constexpr uint32_t kBars = 16 * 8;
-  static constexpr uint32_t kSmem = 1024 + 2 * kStage + kVis + kBars + 16;
+  static constexpr uint32_t kBars = 32 * 8;
+  static constexpr uint32_t kSmem = 1024 + kStages * kStage + kVis + kBars + 16;
 };
 
 // Epilogue factor of one pixel for channel c (mode 0: gradient with chain
@@ -353,73 +413,165 @@ __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int
   return 0.0f;
 }
 
-struct Octet {
-  uint4 hre, him, lre, lim;
-};
+// Two FP32 values in one 64-bit register pair, for the packed FP32x2
+// arithmetic of sm_100-class SMs (one instruction, two lanes of FP32).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 up2(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 
-// 8 consecutive rows of one operand for one visibility: FP16 hi/lo parts of
-// Re and (sign-adjusted) Im, packed for 16-byte stores.
-template <bool kIsB>
-__device__ __forceinline__ Octet gen_octet(const VisEntry& ve, int r0, bool fast) {
+// Start of the recurrence for one visibility at row r0: the phasor v (with
+// the operand's scale or residual folded in), the row step d and the chirp
+// angle eq of d's per-row rotation.  A: b(i) = e^{2 pi i th};  B: the
+// conjugate of x(j) = conj(c) a(j), i.e. c e^{-2 pi i th} with c = w Vr,
+// so that B's second K row (-Im x) is the imaginary part of what is
+// generated.
+template <bool kIsB, bool kFast>
+__device__ __forceinline__ void anchor(const VisEntry& ve, int r0, float2& v, float2& d,
+                                       float& eq) {
   const uint32_t F = kIsB ? ve.FU : ve.FV;
   const float G = kIsB ? ve.GU : ve.GV;
-  const float2 E = kIsB ? ve.Eu : ve.Ev;
+  const float2 E = kIsB ? make_float2(ve.Eu.x, -ve.Eu.y) : ve.Ev;
   const float rf = (float)r0;
   const uint32_t lin = (uint32_t)r0 * F;
-  float th = (float)(int32_t)lin * 2.3283064365386963e-10f;
-  th = fmaf(-rf * rf, G, th);
-  // th is in [-0.5, 0.5] cycles: the SFU's sin/cos of 2 pi th are within
-  // ~4e-7 absolute, below the FP16 hi/lo split's own error budget
+  // th = frac(r0 F / 2^32) - r0^2 G cycles, in [-0.5, 0.5] (negated for B);
+  // the SFU's sin/cos of 2 pi th are within ~4e-7 absolute, below the FP16
+  // hi/lo split's own error budget
+  const float lf = (float)(int32_t)lin * 2.3283064365386963e-10f;
+  const float th = kIsB ? fmaf(rf * rf, G, -lf) : fmaf(-rf * rf, G, lf);
   float sn, cs;
-  if (fast)
+  if (kFast)
     __sincosf(6.283185307179586f * th, &sn, &cs);
   else
     sincospif(2.0f * th, &sn, &cs);
-  float2 v = make_float2(cs, sn);
+  v = make_float2(cs, sn);
   if (kIsB)
     v = cmul(v, ve.c);
   else
     v = make_float2(v.x * ve.ascale, v.y * ve.ascale);
-  // d = e^{2 pi i (f - G (2 r0 + 1))}, q = e^{-4 pi i G}; the chirp angles
-  // are below 1e-3 rad, so second-order expansions are exact in FP32
-  const float eps = -6.283185307179586f * G * (2.0f * rf + 1.0f);
-  float2 d = cmul(E, make_float2(fmaf(-0.5f * eps, eps, 1.0f), eps));
-  const float eq = -12.566370614359172f * G;
-  float re[8], im[8];
-#pragma unroll
-  for (int t = 0; t < 8; t++) {
-    re[t] = v.x;
-    im[t] = kIsB ? -v.y : v.y;
-    if (t < 7) {
-      v = cmul(v, d);
-      d = make_float2(fmaf(-eq, d.y, d.x), fmaf(eq, d.x, d.y));
-    }
-  }
-  uint32_t hre[4], him[4], lre[4], lim[4];
-#pragma unroll
-  for (int t = 0; t < 4; t++) {
-    const __half2 h_re = __floats2half2_rn(re[2 * t], re[2 * t + 1]);
-    const __half2 h_im = __floats2half2_rn(im[2 * t], im[2 * t + 1]);
-    const float2 b_re = __half22float2(h_re);
-    const float2 b_im = __half22float2(h_im);
-    const __half2 l_re = __floats2half2_rn(re[2 * t] - b_re.x, re[2 * t + 1] - b_re.y);
-    const __half2 l_im = __floats2half2_rn(im[2 * t] - b_im.x, im[2 * t + 1] - b_im.y);
-    hre[t] = *reinterpret_cast<const uint32_t*>(&h_re);
-    him[t] = *reinterpret_cast<const uint32_t*>(&h_im);
-    lre[t] = *reinterpret_cast<const uint32_t*>(&l_re);
-    lim[t] = *reinterpret_cast<const uint32_t*>(&l_im);
-  }
-  Octet o;
-  o.hre = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-  o.him = make_uint4(him[0], him[1], him[2], him[3]);
-  o.lre = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-  o.lim = make_uint4(lim[0], lim[1], lim[2], lim[3]);
-  return o;
+  // d = e^{+-2 pi i (f - G (2 r0 + 1))}, rotated by eq = -+4 pi G per row;
+  // the chirp angles are below 1e-3 rad, so second-order expansions are
+  // exact in FP32
+  const float eps0 = 6.283185307179586f * G * (2.0f * rf + 1.0f);
+  const float eps = kIsB ? eps0 : -eps0;
+  d = cmul(E, make_float2(fmaf(-0.5f * eps, eps, 1.0f), eps));
+  eq = kIsB ? 12.566370614359172f * G : -12.566370614359172f * G;
 }
 
-// The chunk sequence every warp of every CTA of a cluster walks in the same
-// order: the cluster's work items (row-tile group, column tile, split), the
-// channels each split overlaps, and 32-visibility chunks within a channel.
+// One generator task: rows 8*oct..8*oct+7 of MN atom `matom` for the
+// visibilities kv0 and kv0 + 4 of the chunk, hi and lo parts.  The two
+// visibilities' recurrences run side by side in packed FP32x2 registers.
+template <bool kIsB, bool kFast>
+__device__ __forceinline__ void gen_task(uint8_t* t_hi, uint8_t* t_lo, uint32_t sbo, int matom,
+                                         int r0, const VisEntry* sv, int kv0, int oct) {
+  float2 va, vb, da, db;
+  float eqa, eqb;
+  anchor<kIsB, kFast>(sv[kv0], r0, va, da, eqa);
+  anchor<kIsB, kFast>(sv[kv0 + 4], r0, vb, db, eqb);
+  f32x2 VR = pk2(va.x, vb.x), VI = pk2(va.y, vb.y);
+  f32x2 DC = pk2(da.x, db.x), DS = pk2(da.y, db.y), NDS = pk2(-da.y, -db.y);
+  const f32x2 EQ = pk2(eqa, eqb), NEQ = pk2(-eqa, -eqb);
+  f32x2 R[8], I[8];
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    R[t] = VR;
+    I[t] = VI;
+    if (t < 7) {
+      // v <- v d;  d <- d (1 + i eq)
+      const f32x2 vr = fma2(VR, DC, mul2(VI, NDS));
+      const f32x2 vi = fma2(VR, DS, mul2(VI, DC));
+      const f32x2 dc = fma2(NEQ, DS, DC);
+      const f32x2 ds = fma2(EQ, DC, DS);
+      NDS = fma2(NEQ, DC, NDS);
+      VR = vr;
+      VI = vi;
+      DC = dc;
+      DS = ds;
+    }
+  }
+  // FP16 hi = rn(x), lo = rn(x - hi), rows paired for the 16-byte stores
+  uint32_t hre[2][4], him[2][4], lre[2][4], lim[2][4];
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    {
+      const float2 x0 = up2(R[2 * t]), x1 = up2(R[2 * t + 1]);
+      const __half2 ha = __floats2half2_rn(x0.x, x1.x), hb = __floats2half2_rn(x0.y, x1.y);
+      const float2 fa = __half22float2(ha), fb = __half22float2(hb);
+      const float2 l0 = up2(sub2(R[2 * t], pk2(fa.x, fb.x)));
+      const float2 l1 = up2(sub2(R[2 * t + 1], pk2(fa.y, fb.y)));
+      hre[0][t] = h2u(ha);
+      hre[1][t] = h2u(hb);
+      lre[0][t] = h2u(__floats2half2_rn(l0.x, l1.x));
+      lre[1][t] = h2u(__floats2half2_rn(l0.y, l1.y));
+    }
+    {
+      const float2 x0 = up2(I[2 * t]), x1 = up2(I[2 * t + 1]);
+      const __half2 ha = __floats2half2_rn(x0.x, x1.x), hb = __floats2half2_rn(x0.y, x1.y);
+      const float2 fa = __half22float2(ha), fb = __half22float2(hb);
+      const float2 l0 = up2(sub2(I[2 * t], pk2(fa.x, fb.x)));
+      const float2 l1 = up2(sub2(I[2 * t + 1], pk2(fa.y, fb.y)));
+      him[0][t] = h2u(ha);
+      him[1][t] = h2u(hb);
+      lim[0][t] = h2u(__floats2half2_rn(l0.x, l1.x));
+      lim[1][t] = h2u(__floats2half2_rn(l0.y, l1.y));
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 2; v++) {
+    const int kv = kv0 + 4 * v;
+    const uint32_t ore = tile_off(matom, oct, 2 * kv, sbo);
+    const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, sbo);
+    *reinterpret_cast<uint4*>(t_hi + ore) = make_uint4(hre[v][0], hre[v][1], hre[v][2], hre[v][3]);
+    *reinterpret_cast<uint4*>(t_hi + oim) = make_uint4(him[v][0], him[v][1], him[v][2], him[v][3]);
+    *reinterpret_cast<uint4*>(t_lo + ore) = make_uint4(lre[v][0], lre[v][1], lre[v][2], lre[v][3]);
+    *reinterpret_cast<uint4*>(t_lo + oim) = make_uint4(lim[v][0], lim[v][1], lim[v][2], lim[v][3]);
+  }
+}
+
+// running sum += accumulator over `ncols` columns from `col0` (one TMEM lane
+// quarter per warp)
+__device__ __forceinline__ void drain_cols(uint32_t t_acc, uint32_t t_run, uint32_t lane_off,
+                                           int col0, int ncols, bool run_empty) {
+#pragma unroll 1
+  for (int cb = 0; cb < ncols; cb += 32) {
+    const uint32_t col = (uint32_t)(col0 + cb);
+    float acc[32], run[32];
+    tmem_ld32(t_acc + lane_off + col, acc);
+    if (!run_empty) {
+      tmem_ld32(t_run + lane_off + col, run);
+#pragma unroll
+      for (int k = 0; k < 32; k++) acc[k] += run[k];
+    }
+    tmem_st32(t_run + lane_off + col, acc);
+  }
+}
+
+// The chunk sequence every warp of both CTAs of a pair walks in the same
+// order: the work items (row-tile group, column tile, split), the channels
+// each split overlaps, and 32-visibility chunks within a channel.
 struct ChunkIter {
   int item, c, n, nchunks;
   int64_t goff, nvis;
@@ -434,8 +586,8 @@ __device__ __forceinline__ void item_range(const TcParams& p, int item, int64_t*
 }
 
 // position `it` on the first chunk at or after (item, channel c); returns
-// false when the cluster has no more chunks
-__device__ bool iter_seek(const TcParams& p, int nitems, int stride, ChunkIter& it) {
+// false when there are no more chunks
+__device__ __forceinline__ bool iter_seek(const TcParams& p, int nitems, int stride, ChunkIter& it) {
   while (it.item < nitems) {
     int64_t ks, ke;
     item_range(p, it.item, &ks, &ke);
@@ -460,59 +612,65 @@ __device__ bool iter_seek(const TcParams& p, int nitems, int stride, ChunkIter& 
 
 __device__ __forceinline__ void iter_next(const TcParams& p, int nitems, int stride,
                                           ChunkIter& it) {
+  if (!it.valid) return;
   if (++it.n < it.nchunks) return;
   it.c++;
   iter_seek(p, nitems, stride, it);
 }
 
-template <int TN, int CS, int VPL>
-__global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p) {
-  using L = Layout<TN>;
-  constexpr int GW = gen_warps(CS, VPL);
-  constexpr int kMB = TN / 64;        // MN atoms of B
-  constexpr int kMBown = kMB / CS;    // B atoms this CTA generates
+template <int TN, bool PAIR>
+__global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
+  using L = Layout<TN, PAIR>;
+  constexpr int S = L::kStages;
+  constexpr int NH = TN / 2;  // accumulator columns per half
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + 2 * L::kStage);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + 2 * L::kStage + L::kVis);
-  uint64_t* op_full = bars;       // [2]  one arrive per generator warp per CTA of the cluster
-  uint64_t* op_empty = bars + 2;  // [2]  one MMA commit per CTA of the cluster
-  uint64_t* vis_full = bars + 4;  // [4]  32 arrives (control lanes)
-  uint64_t* vis_empty = bars + 8; // [4]  one arrive per generator warp
-  uint64_t* drained = bars + 12;  // [1]  one arrive per draining warp
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 16);
+  VisEntry* s_vis = reinterpret_cast<VisEntry*>(base + S * L::kStage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + S * L::kStage + L::kVis);
+  uint64_t* op_full = bars;        // [S]  one arrive per generator warp of the pair (leader)
+  uint64_t* op_empty = bars + 3;   // [S]  one MMA commit
+  uint64_t* vis_full = bars + 6;   // [6]  32 arrives (control lanes)
+  uint64_t* vis_empty = bars + 12; // [6]  one arrive per generator warp
+  uint64_t* acc0_done = bars + 18; // [1]  MMA commit after the first accumulator half
+  uint64_t* drained = bars + 19;   // [2]  one arrive per drain warp of the pair (leader)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 24);
   __shared__ int s_abort;
   volatile int* abort = &s_abort;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t rank = CS > 1 ? cluster_rank() : 0u;
-  const int cid = CS > 1 ? (int)cluster_id() : (int)blockIdx.x;
-  const int ncl = CS > 1 ? (int)num_clusters() : (int)gridDim.x;
+  const uint32_t rank = PAIR ? cluster_rank() : 0u;
+  const bool leader = rank == 0u;
+  const int cid = PAIR ? (int)cluster_id() : (int)blockIdx.x;
+  const int ncl = PAIR ? (int)num_clusters() : (int)gridDim.x;
   if (warp == 0) {
-    tmem_alloc(tslot, kTmemCols);
-    tmem_relinquish();
+    tmem_alloc<PAIR>(tslot, kTmemCols);
+    tmem_relinquish<PAIR>();
   }
   if (tid == 0) {
-    mbar_init(&op_full[0], GW * CS);
-    mbar_init(&op_full[1], GW * CS);
-    mbar_init(&op_empty[0], CS);
-    mbar_init(&op_empty[1], CS);
+    const uint32_t peers = PAIR ? 2u : 1u;
+    for (int s = 0; s < S; s++) {
+      // local generator warps, plus the peer's forwarded arrive in the leader
+      mbar_init(&op_full[s], kGW + ((PAIR && rank == 0u) ? 1u : 0u));
+      mbar_init(&op_empty[s], 1);
+    }
     for (int s = 0; s < kVisSlots; s++) {
       mbar_init(&vis_full[s], 32);
-      mbar_init(&vis_empty[s], GW);
+      mbar_init(&vis_empty[s], kGW);
     }
-    mbar_init(drained, kDrainWarps);
+    mbar_init(acc0_done, 1);
+    mbar_init(&drained[0], kDW * peers);
+    mbar_init(&drained[1], kDW * peers);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   fence_before();
   __syncthreads();
-  if (CS > 1) cluster_sync();  // peers' barriers are initialised before any remote access
+  if (PAIR) cluster_sync();  // the peer's barriers are initialised before any remote arrive
   fence_after();
   const uint32_t tbase = *tslot;
   const uint32_t t_acc = tbase;
-  const uint32_t t_run = tbase + 256;
+  const uint32_t t_run = tbase + TN;
 
   // operand scale: c * 2^-e with max |c| * 2^-e <= 1
   const float cmax = __uint_as_float(*p.cmax_bits);
@@ -520,44 +678,60 @@ __global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p
   if (cmax > 0.0f) frexpf(cmax, &e);
   const float scale = ldexpf(1.0f, -e);
   const float inv_s = ldexpf(1.0f, e);
-  const int nitems = (p.ntile_i / CS) * p.ntile_j * p.nsplit;
-  uint32_t nch = 0;  // position in the cluster's chunk sequence
+  constexpr int kRowsPerItem = PAIR ? 2 : 1;
+  const int nitems = (p.ntile_i / kRowsPerItem) * p.ntile_j * p.nsplit;
+  uint32_t nch = 0;  // position in the chunk sequence
 
-  if (warp == GW) {
-    // ------------------------------- control warp --------------------------
-    ChunkIter ld{cid, 0, 0, 0, 0, 0, false};
-    ChunkIter mm = ld;
-    iter_seek(p, nitems, ncl, ld);
-    iter_seek(p, nitems, ncl, mm);
-    uint32_t nld = 0, ndrain = 0;
-    const uint32_t idesc = make_idesc(kTM, TN);
-    bool ok = true;
-    auto load_one = [&](const ChunkIter& it, uint32_t q) -> bool {
-      const int slot = q % kVisSlots;
-      if (q >= kVisSlots) {
-        if (!mbar_wait(&vis_empty[slot], ((q / kVisSlots) - 1) & 1, abort, p.err, 4u)) return false;
-      }
-      VisEntry ve;
+  if (warp == kGW + kDW) {
+    // ------------------------------- loader warp ---------------------------
+    // Visibility constants are fetched two chunks before they are stored
+    // into the ring, so the global-memory latency overlaps the wait for a
+    // free slot.
+    struct VisRaw {
+      uint4 ph;
+      float4 E, d;  // d: deg (dirty image only)
+      float2 r;     // cvr, or vo (dirty image)
+      bool valid;
+    };
+    auto fetch = [&](const ChunkIter& it) -> VisRaw {
+      VisRaw r;
       const int64_t kidx = (int64_t)it.n * kChunkVis + lane;
-      if (kidx < it.nvis) {
+      r.valid = it.valid && kidx < it.nvis;
+      if (r.valid) {
         const int64_t g = it.goff + kidx;
-        const uint4 ph = p.ph[g];
-        const float4 E = p.E[g];
-        float2 cc;
+        r.ph = p.ph[g];
+        r.E = p.E[g];
         if (p.mode == 2) {
-          const float4 d = p.deg[g];
-          const float2 o = p.vo[g];
-          cc = make_float2(d.w * o.x, -(d.w * o.y));
+          r.d = p.deg[g];
+          r.r = p.vo[g];
         } else {
-          const float2 r = p.cvr[g];
-          cc = make_float2(r.x, -r.y);
+          r.r = p.cvr[g];
         }
-        ve.FU = ph.x;
-        ve.FV = ph.y;
-        ve.GU = __uint_as_float(ph.z);
-        ve.GV = __uint_as_float(ph.w);
-        ve.Eu = make_float2(E.x, E.y);
-        ve.Ev = make_float2(E.z, E.w);
+      }
+      return r;
+    };
+    ChunkIter ld{cid, 0, 0, 0, 0, 0, false};
+    iter_seek(p, nitems, ncl, ld);
+    ChunkIter fi = ld;  // next chunk to fetch
+    VisRaw ra = fetch(fi);
+    iter_next(p, nitems, ncl, fi);
+    VisRaw rb = fetch(fi);
+    iter_next(p, nitems, ncl, fi);
+    uint32_t nld = 0;
+    while (ld.valid) {
+      const int slot = nld % kVisSlots;
+      if (nld >= (uint32_t)kVisSlots &&
+          !warp_wait(&vis_empty[slot], ((nld / kVisSlots) - 1) & 1, abort, p.err, 4u))
+        break;
+      VisEntry ve;
+      if (ra.valid) {
+        const float2 cc = p.mode == 2 ? make_float2(ra.d.w * ra.r.x, ra.d.w * ra.r.y) : ra.r;
+        ve.FU = ra.ph.x;
+        ve.FV = ra.ph.y;
+        ve.GU = __uint_as_float(ra.ph.z);
+        ve.GV = __uint_as_float(ra.ph.w);
+        ve.Eu = make_float2(ra.E.x, ra.E.y);
+        ve.Ev = make_float2(ra.E.z, ra.E.w);
         ve.c = make_float2(cc.x * scale, cc.y * scale);
       } else {
         ve.FU = ve.FV = 0u;
@@ -565,114 +739,107 @@ __global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p
         ve.Eu = ve.Ev = make_float2(1.0f, 0.0f);
         ve.c = make_float2(0.0f, 0.0f);
       }
-      // chunk scale: B carries c / 2^e, A carries b * 2^e (powers of two,
+      // chunk scale 2^ce, ce = frexp exponent of the chunk's max |c| clamped
+      // to [-24, 0]: B carries c / 2^ce, A carries b * 2^ce (powers of two,
       // exact), so small residuals keep FP16's relative precision
       float m = fmaxf(fabsf(ve.c.x), fabsf(ve.c.y));
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-      int ce = 0;
-      if (m > 0.0f) frexpf(m, &ce);
+      int ce = (int)((__float_as_uint(m) >> 23) & 0xffu) - 126;
       ce = ce < -24 ? -24 : (ce > 0 ? 0 : ce);
-      ve.ascale = ldexpf(1.0f, ce);
-      ve.c = make_float2(ldexpf(ve.c.x, -ce), ldexpf(ve.c.y, -ce));
+      ve.ascale = __uint_as_float((uint32_t)(127 + ce) << 23);
+      const float up = __uint_as_float((uint32_t)(127 - ce) << 23);
+      ve.c = make_float2(ve.c.x * up, ve.c.y * up);
       ve.pad = 0.0f;
       s_vis[slot * kChunkVis + lane] = ve;
       mbar_arrive(&vis_full[slot]);
-      return true;
-    };
-    // prime the ring
-    while (ok && ld.valid && nld < (uint32_t)kLookahead) {
-      ok = load_one(ld, nld);
       nld++;
       iter_next(p, nitems, ncl, ld);
+      ra = rb;
+      rb = fetch(fi);
+      iter_next(p, nitems, ncl, fi);
     }
-    while (ok && mm.valid) {
-      if (ld.valid) {
-        ok = load_one(ld, nld);
-        nld++;
-        iter_next(p, nitems, ncl, ld);
+  } else if (warp == kGW + kDW + 1) {
+    // --------------------------------- MMA warp ----------------------------
+    // Leader CTA: lane 0 issues the MMAs of each full stage.  Peer CTA: lane
+    // 0 forwards the completion of its local stage to the leader, one
+    // cluster-scope arrive per chunk.
+    if (lane == 0) {
+      ChunkIter mm{cid, 0, 0, 0, 0, 0, false};
+      iter_seek(p, nitems, ncl, mm);
+      const uint32_t idesc = make_idesc(PAIR ? 2 * kTM : kTM, NH);
+      // descriptor words: low = start address >> 4 | (LBO = 1024) >> 4 << 16,
+      // high = SBO >> 4 | version 1 | 128-byte swizzle
+      const uint32_t lo0 = (smem_u32(base) >> 4) | (64u << 16);
+      const uint32_t hiA = (L::kSboA >> 4) | (1u << 14) | (2u << 29);
+      const uint32_t hiB = (L::kSboB >> 4) | (1u << 14) | (2u << 29);
+      auto desc = [](uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; };
+      uint32_t ndrain = 0;
+      bool ok = true;
+      while (ok && mm.valid) {
+        const int st = (int)(nch % S);
+        const bool fresh = (mm.n % p.slab) == 0;
+        const bool drain = (mm.n == mm.nchunks - 1) || ((mm.n % p.slab) == p.slab - 1);
+        ok = mbar_wait(&op_full[st], (nch / S) & 1, abort, p.err, 5u);
         if (!ok) break;
-      }
-      const int st = nch & 1;
-      const bool fresh = (mm.n % p.slab) == 0;
-      const bool drain = (mm.n == mm.nchunks - 1) || ((mm.n % p.slab) == p.slab - 1);
-      if (lane == 0) {
-        ok = mbar_wait(&op_full[st], (nch >> 1) & 1, abort, p.err, 5u);
-        if (ok && fresh && nch > 0) ok = mbar_wait(drained, (ndrain - 1) & 1, abort, p.err, 6u);
-        if (ok) {
-          fence_after();
-          uint8_t* sp = base + st * L::kStage;
-          const uint32_t sa_hi = smem_u32(sp), sa_lo = sa_hi + L::kTileA;
-          const uint32_t sb_hi = sa_hi + 2 * L::kTileA, sb_lo = sb_hi + L::kTileB;
+        if (PAIR && !leader) {
+          arrive_leader<PAIR>(&op_full[st]);
+        } else {
+          const uint32_t lw = lo0 + (uint32_t)st * (L::kStage >> 4);
 #pragma unroll
-          for (int t = 0; t < kKC / 16; t++) {
-            const uint64_t ah = make_desc(sa_hi + t * 2 * L::kSboA, 1024, L::kSboA);
-            const uint64_t al = make_desc(sa_lo + t * 2 * L::kSboA, 1024, L::kSboA);
-            const uint64_t bh = make_desc(sb_hi + t * 2 * L::kSboB, 1024, L::kSboB);
-            const uint64_t bl = make_desc(sb_lo + t * 2 * L::kSboB, 1024, L::kSboB);
-            mma_f16(t_acc, ah, bh, idesc, (fresh && t == 0) ? 0u : 1u);
-            mma_f16(t_acc, ah, bl, idesc, 1u);
-            mma_f16(t_acc, al, bh, idesc, 1u);
+          for (int h = 0; h < 2; h++) {
+            if (fresh && nch > 0) ok = mbar_wait(&drained[h], (ndrain - 1) & 1, abort, p.err, 6u);
+            if (!ok) break;
+            fence_after();
+            const uint32_t d = t_acc + (uint32_t)(h * NH);
+            constexpr uint32_t kB = 2 * L::kTileA;
+            const uint32_t boff = (uint32_t)(h * L::kHatoms * 1024);
+#pragma unroll
+            for (int t = 0; t < kKC / 16; t++) {
+              const uint64_t ah = desc(lw + ((t * 2 * L::kSboA) >> 4), hiA);
+              const uint64_t al = desc(lw + ((L::kTileA + t * 2 * L::kSboA) >> 4), hiA);
+              const uint64_t bh = desc(lw + ((kB + boff + t * 2 * L::kSboB) >> 4), hiB);
+              const uint64_t bl = desc(lw + ((kB + L::kTileB + boff + t * 2 * L::kSboB) >> 4), hiB);
+              mma_f16<PAIR>(d, ah, bh, idesc, (fresh && t == 0) ? 0u : 1u);
+              mma_f16<PAIR>(d, ah, bl, idesc, 1u);
+              mma_f16<PAIR>(d, al, bh, idesc, 1u);
+            }
+            if (h == 0 && drain) mma_commit<PAIR>(acc0_done);
           }
-          if (CS > 1)
-            mma_commit_multicast(&op_empty[st], (uint16_t)((1u << CS) - 1u));
-          else
-            mma_commit(&op_empty[st]);
+          if (ok) mma_commit<PAIR>(&op_empty[st]);
         }
+        if (drain) ndrain++;
+        nch++;
+        iter_next(p, nitems, ncl, mm);
       }
-      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-      if (drain) ndrain++;
-      nch++;
-      iter_next(p, nitems, ncl, mm);
-    }
-    // retire: no MMA of this CTA may be in flight when TMEM is freed (the
-    // barrier also counts the peers' commits, which only makes this later)
-    if (lane == 0 && nch > 0) {
-      const uint32_t q = nch - 1;
-      const long long t0 = clock64();
-      while (!mbar_try_wait(&op_empty[q & 1], (q >> 1) & 1)) {
-        if (clock64() - t0 > kWaitCycles) {
-          atomicExch(p.err, 7u);
-          break;
+      // retire: no MMA may be in flight when TMEM is freed
+      if (leader && nch > 0) {
+        const uint32_t q = nch - 1;
+        const long long t0 = clock64();
+        while (!mbar_try_wait(&op_empty[q % S], (q / S) & 1)) {
+          if (clock64() - t0 > kWaitCycles) {
+            atomicExch(p.err, 7u);
+            break;
+          }
         }
       }
     }
-  } else {
-    // ----------------------------- generator warps -------------------------
-    const int oct = lane & 7, kq = lane >> 3;
-    const bool fast = p.fast_anchor != 0;
-    constexpr int kVq = kChunkVis / (4 * VPL);  // visibility groups per chunk
-    constexpr int kTasksA = (kTM / 64) * kVq;
-    constexpr int kTasksB = kMBown * kVq;
-    constexpr int kCols = TN / 2;             // epilogue columns per draining thread
-    const bool drainer = warp < kDrainWarps;
-    const int lq = warp & 3, half = (warp >> 2) & 1;
+  } else if (warp >= kGW) {
+    // ------------------------------- drain warps ---------------------------
+    const int lq = warp & 3;
     const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
-    // shared::cluster addresses of both stages' B tiles and op_full barriers
-    // in every CTA of the cluster
-    uint32_t bhi_r[2][CS], blo_r[2][CS], full_r[2][CS];
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      const uint32_t lb = smem_u32(base + s * L::kStage + 2 * L::kTileA);
-#pragma unroll
-      for (int r = 0; r < CS; r++) {
-        bhi_r[s][r] = CS > 1 ? map_rank(lb, r) : lb;
-        blo_r[s][r] = CS > 1 ? map_rank(lb + L::kTileB, r) : lb + L::kTileB;
-        full_r[s][r] = CS > 1 ? map_rank(smem_u32(&op_full[s]), r) : smem_u32(&op_full[s]);
-      }
-    }
+    uint32_t ndr = 0;
     bool ok = true;
     for (int item = cid; item < nitems && ok; item += ncl) {
       const int split = item % p.nsplit;
       const int tile = item / p.nsplit;
       const int tig = tile / p.ntile_j, tj = tile % p.ntile_j;
-      const int i0 = (tig * CS + (int)rank) * kTM, j0 = tj * TN;
+      const int i0 = (tig * kRowsPerItem + (int)rank) * kTM, j0 = tj * TN;
       int64_t ks, ke;
       item_range(p, item, &ks, &ke);
       bool first_channel = true;
       const int ei = i0 + 32 * lq + lane;
-      const int ej0 = j0 + half * kCols;
-      float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + ej0;
+      float* prow = p.partial + (int64_t)split * p.MN + (int64_t)p.N * ei + j0;
       for (int c = 0; c < p.C && ok; c++) {
         const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
         const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
@@ -680,106 +847,34 @@ __global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p
         const int nchunks = (int)((b - a + kChunkVis - 1) / kChunkVis);
         bool run_empty = true;
         for (int n = 0; n < nchunks && ok; n++) {
-          const int st = nch & 1;
-          const int slot = nch % kVisSlots;
-          if (nch >= 2) ok = warp_wait(&op_empty[st], ((nch >> 1) - 1) & 1, abort, p.err, 1u);
-          if (ok) ok = warp_wait(&vis_full[slot], (nch / kVisSlots) & 1, abort, p.err, 2u);
-          if (!ok) break;
-          uint8_t* sp = base + st * L::kStage;
-          uint8_t* a_hi = sp;
-          uint8_t* a_lo = sp + L::kTileA;
-          const VisEntry* sv = s_vis + slot * kChunkVis;
-          for (int wt = warp; wt < kTasksA + kTasksB; wt += GW) {
-            if (wt < kTasksA) {
-              const int matom = wt / kVq;
-              const int kv0 = (wt % kVq) * 4 * VPL + kq;
-              const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
-              Octet o[VPL];
-#pragma unroll
-              for (int v = 0; v < VPL; v++) o[v] = gen_octet<false>(sv[kv0 + 4 * v], r0, fast);
-#pragma unroll
-              for (int v = 0; v < VPL; v++) {
-                const int kv = kv0 + 4 * v;
-                const uint32_t ore = tile_off(matom, oct, 2 * kv, L::kSboA);
-                const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, L::kSboA);
-                *reinterpret_cast<uint4*>(a_hi + ore) = o[v].hre;
-                *reinterpret_cast<uint4*>(a_hi + oim) = o[v].him;
-                *reinterpret_cast<uint4*>(a_lo + ore) = o[v].lre;
-                *reinterpret_cast<uint4*>(a_lo + oim) = o[v].lim;
-              }
-            } else {
-              const int w2 = wt - kTasksA;
-              const int matom = (int)rank * kMBown + w2 / kVq;
-              const int kv0 = (w2 % kVq) * 4 * VPL + kq;
-              const int r0 = j0 + matom * 64 + oct * 8 - p.x0;
-              Octet o[VPL];
-#pragma unroll
-              for (int v = 0; v < VPL; v++) o[v] = gen_octet<true>(sv[kv0 + 4 * v], r0, fast);
-#pragma unroll
-              for (int v = 0; v < VPL; v++) {
-                const int kv = kv0 + 4 * v;
-                const uint32_t ore = tile_off(matom, oct, 2 * kv, L::kSboB);
-                const uint32_t oim = tile_off(matom, oct, 2 * kv + 1, L::kSboB);
-                if (CS == 1) {
-                  uint8_t* b_hi = sp + 2 * L::kTileA;
-                  uint8_t* b_lo = b_hi + L::kTileB;
-                  *reinterpret_cast<uint4*>(b_hi + ore) = o[v].hre;
-                  *reinterpret_cast<uint4*>(b_hi + oim) = o[v].him;
-                  *reinterpret_cast<uint4*>(b_lo + ore) = o[v].lre;
-                  *reinterpret_cast<uint4*>(b_lo + oim) = o[v].lim;
-                } else {
-#pragma unroll
-                  for (int r = 0; r < CS; r++) {
-                    st_cluster_v4(bhi_r[st][r] + ore, o[v].hre);
-                    st_cluster_v4(bhi_r[st][r] + oim, o[v].him);
-                    st_cluster_v4(blo_r[st][r] + ore, o[v].lre);
-                    st_cluster_v4(blo_r[st][r] + oim, o[v].lim);
-                  }
-                }
-              }
-            }
-          }
-          fence_proxy_async();
-          __syncwarp();
-          if (lane == 0) {
-#pragma unroll
-            for (int r = 0; r < CS; r++) mbar_arrive_cluster(full_r[st][r]);
-          }
-          warp_arrive(&vis_empty[slot]);
+          const uint32_t my = nch++;
           const bool last = (n == nchunks - 1);
-          const bool drain = last || ((n % p.slab) == p.slab - 1);
-          const uint32_t my = nch;
-          nch++;
-          if (!drain || !drainer) continue;
-          ok = warp_wait(&op_empty[my & 1], (my >> 1) & 1, abort, p.err, 3u);
+          if (!last && (n % p.slab) != p.slab - 1) continue;
+          // first half: its MMAs are committed before the second half's
+          ok = warp_wait(acc0_done, ndr & 1, abort, p.err, 3u);
           if (!ok) break;
           fence_after();
-          // running sum += accumulator (short FP32 chains)
-#pragma unroll 1
-          for (int cb = 0; cb < kCols; cb += 32) {
-            const uint32_t col = (uint32_t)(half * kCols + cb);
-            float acc[32], run[32];
-            tmem_ld32(t_acc + lane_off + col, acc);
-            if (!run_empty) {
-              tmem_ld32(t_run + lane_off + col, run);
-#pragma unroll
-              for (int k = 0; k < 32; k++) acc[k] += run[k];
-            }
-            tmem_st32(t_run + lane_off + col, acc);
-          }
-          run_empty = false;
+          drain_cols(t_acc, t_run, lane_off, 0, NH, run_empty);
           fence_before();
-          warp_arrive(drained);
+          warp_arrive_leader<PAIR>(&drained[0]);
+          // second half: the chunk's final commit
+          ok = warp_wait(&op_empty[my % S], (my / S) & 1, abort, p.err, 8u);
+          if (!ok) break;
+          fence_after();
+          drain_cols(t_acc, t_run, lane_off, NH, NH, run_empty);
+          fence_before();
+          warp_arrive_leader<PAIR>(&drained[1]);
+          ndr++;
+          run_empty = false;
           if (last) {
             // channel epilogue: partial (+)= factor * running sum
 #pragma unroll 1
-            for (int cb = 0; cb < kCols; cb += 32) {
-              const uint32_t col = (uint32_t)(half * kCols + cb);
+            for (int cb = 0; cb < TN; cb += 32) {
               float run[32];
-              tmem_ld32(t_run + lane_off + col, run);
+              tmem_ld32(t_run + lane_off + (uint32_t)cb, run);
 #pragma unroll 4
               for (int k = 0; k < 32; k++) {
-                const float f = epi_factor(p, c, ei, ej0 + cb + k, inv_s);
+                const float f = epi_factor(p, c, ei, j0 + cb + k, inv_s);
                 const float v = f * run[k];
                 if (first_channel)
                   prow[cb + k] = v;
@@ -791,17 +886,82 @@ __global__ void __launch_bounds__(threads_for(CS, VPL), 1) k_dchi2_tc(TcParams p
           }
         }
       }
-      if (ok && first_channel && drainer) {
+      if (ok && first_channel) {
         // no visibilities in this split for this tile: its partial is zero
-        for (int k = 0; k < kCols; k++) prow[k] = 0.0f;
+        for (int k = 0; k < TN; k++) prow[k] = 0.0f;
+      }
+    }
+  } else {
+    // ----------------------------- generator warps -------------------------
+    const int oct = lane & 7, kq = lane >> 3;
+    const bool fast = p.fast_anchor != 0;
+    constexpr int kVq = kChunkVis / (4 * kVPL);  // visibility groups per chunk
+    constexpr int kTasksA = (kTM / 64) * kVq;
+    constexpr int kTasksB = L::kBatoms * kVq;
+    static_assert(kTasksA == kGW && kTasksB % kGW == 0, "generator task split");
+    bool ok = true;
+    for (int item = cid; item < nitems && ok; item += ncl) {
+      const int tile = item / p.nsplit;
+      const int tig = tile / p.ntile_j, tj = tile % p.ntile_j;
+      const int i0 = (tig * kRowsPerItem + (int)rank) * kTM, j0 = tj * TN;
+      int64_t ks, ke;
+      item_range(p, item, &ks, &ke);
+      for (int c = 0; c < p.C && ok; c++) {
+        const int64_t cs = p.kc_off[c], ce = p.kc_off[c + 1];
+        const int64_t a = ks > cs ? ks : cs, b = ke < ce ? ke : ce;
+        if (a >= b) continue;
+        const int nchunks = (int)((b - a + kChunkVis - 1) / kChunkVis);
+        for (int n = 0; n < nchunks && ok; n++) {
+          const int st = (int)(nch % S);
+          const int slot = (int)(nch % kVisSlots);
+          if (nch >= (uint32_t)S) ok = warp_wait(&op_empty[st], ((nch / S) - 1) & 1, abort, p.err, 1u);
+          if (ok) ok = warp_wait(&vis_full[slot], (nch / kVisSlots) & 1, abort, p.err, 2u);
+          if (!ok) break;
+          uint8_t* sp = base + st * L::kStage;
+          uint8_t* a_hi = sp;
+          uint8_t* a_lo = sp + L::kTileA;
+          uint8_t* b_hi = sp + 2 * L::kTileA;
+          uint8_t* b_lo = b_hi + L::kTileB;
+          const VisEntry* sv = s_vis + slot * kChunkVis;
+          // every warp makes one A task and kTasksB / kGW B tasks, in one
+          // straight-line block
+          auto gen_chunk = [&](auto fast_tag) {
+            constexpr bool kFast = decltype(fast_tag)::value;
+            {
+              const int matom = warp / kVq;
+              const int kv0 = (warp % kVq) * 4 * kVPL + kq;
+              const int r0 = i0 + matom * 64 + oct * 8 - p.y0;
+              gen_task<false, kFast>(a_hi, a_lo, L::kSboA, matom, r0, sv, kv0, oct);
+            }
+#pragma unroll
+            for (int k = 0; k < kTasksB / kGW; k++) {
+              const int w2 = warp + k * kGW;
+              const int batom = w2 / kVq;
+              const int kv0 = (w2 % kVq) * 4 * kVPL + kq;
+              // global column of this atom within the TN-wide tile
+              const int col = (batom / L::kHatoms) * NH + (PAIR ? (int)rank * (NH / 2) : 0) +
+                              (batom % L::kHatoms) * 64;
+              const int r0 = j0 + col + oct * 8 - p.x0;
+              gen_task<true, kFast>(b_hi, b_lo, L::kSboB, batom, r0, sv, kv0, oct);
+            }
+          };
+          if (fast)
+            gen_chunk(std::true_type{});
+          else
+            gen_chunk(std::false_type{});
+          fence_proxy_async();
+          warp_arrive(&op_full[st]);
+          warp_arrive(&vis_empty[slot]);
+          nch++;
+        }
       }
     }
   }
   fence_before();
   __syncthreads();
-  if (CS > 1) cluster_sync();  // no CTA leaves while a peer may still write into it
+  if (PAIR) cluster_sync();  // no CTA leaves while its peer may still use its memory
   fence_after();
-  if (warp == 0) tmem_dealloc(tbase, kTmemCols);
+  if (warp == 0) tmem_dealloc<PAIR>(tbase, kTmemCols);
 }
 
 // result[plane][q] += sum_s partial[s][q] (FP64, fixed order)
@@ -814,35 +974,36 @@ __global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restric
   out[q] += (float)s;
 }
 
-template <int TN, int CS, int VPL>
+template <int TN, bool PAIR>
 gv_status launch_tc(const Problem& P, const TcParams& p, int nitems) {
-  auto kern = k_dchi2_tc<TN, CS, VPL>;
-  const size_t smem = Layout<TN>::kSmem;
+  auto kern = k_dchi2_tc<TN, PAIR>;
+  const size_t smem = Layout<TN, PAIR>::kSmem;
   GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
-  cfg.blockDim = dim3(threads_for(CS, VPL), 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = P.stream;
-  int nclusters = P.num_sms / CS;
-  if (CS > 1) {
+  const int cs = PAIR ? 2 : 1;
+  int nclusters = P.num_sms / cs;
+  if (PAIR) {
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CS;
+    attr[0].val.clusterDim.x = 2;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cfg.gridDim = dim3(CS * nclusters, 1, 1);
+    cfg.gridDim = dim3(2 * nclusters, 1, 1);
     int active = 0;
     GV_CUDA(cudaOccupancyMaxActiveClusters(&active, kern, &cfg));
     if (active <= 0) {
-      set_error("no cluster of the tensor-core DChi2 kernel fits on this device");
+      set_error("no CTA pair of the tensor-core DChi2 kernel fits on this device");
       return GV_ERR_UNSUPPORTED;
     }
     nclusters = std::min(nclusters, active);
   }
   nclusters = std::max(1, std::min(nclusters, nitems));
-  cfg.gridDim = dim3(CS * nclusters, 1, 1);
+  cfg.gridDim = dim3(cs * nclusters, 1, 1);
   GV_CUDA(cudaLaunchKernelEx(&cfg, kern, p));
   GV_LAUNCH("k_dchi2_tc");
   return GV_OK;
@@ -856,18 +1017,12 @@ bool dchi2_tc_supported(const Problem& P) {
 
 int tc_tile_n(const Problem& P) { return P.N >= 256 ? 256 : 128; }
 
-// cluster size: the largest of 4, 2, 1 dividing the row tiles and the B atoms
-int tc_cluster(const Problem& P) {
-  const int TN = tc_tile_n(P);
-  const int ntile_i = P.N / tc::kTM;
-  // measured on GB300 (2048^2, 35.28M visibilities): 1 CTA 2.30 s, clusters
-  // of 2 3.44 s, of 4 5.48 s -- the remote 16-byte stores of the shared B
-  // tile cost more than the generation they save -- so clusters are opt-in
-  int cs = 1;
-  const char* env = std::getenv("GV_TC_CLUSTER");
-  if (env) cs = std::atoi(env);
-  while (cs > 1 && (ntile_i % cs != 0 || (TN / 64) % cs != 0 || (cs != 2 && cs != 4))) cs /= 2;
-  return cs < 1 ? 1 : cs;
+// CTA pairs (cta_group::2) for images of side >= 256; GV_TC_PAIR=0 selects
+// single CTAs
+bool tc_pair(const Problem& P) {
+  if (P.N < 256) return false;
+  const char* e = std::getenv("GV_TC_PAIR");
+  return !(e && e[0] == '0');
 }
 
 gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result,
@@ -901,7 +1056,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.slab = sl ? std::max(1, std::atoi(sl)) : tc::kSlab;
   }
   const int TN = tc_tile_n(P);
-  const int CS = tc_cluster(P);
+  const bool pair = tc_pair(P);
   p.ntile_i = P.N / tc::kTM;
   p.ntile_j = P.N / TN;
   p.nsplit = P.tc_nsplit;
@@ -930,21 +1085,12 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.kc_off = P.d_kc_off;
     p.Ktot = P.Vgrid;
   }
-  const int nitems = (p.ntile_i / CS) * p.ntile_j * p.nsplit;
-  // visibilities per generator lane (independent chains for ILP)
-  int vpl = 2;
-  if (const char* v = std::getenv("GV_TC_VPL")) vpl = std::atoi(v) == 1 ? 1 : 2;
+  const int nitems = (p.ntile_i / (pair ? 2 : 1)) * p.ntile_j * p.nsplit;
   gv_status s;
-  if (TN == 256) {
-    if (CS == 4) s = tc::launch_tc<256, 4, 1>(P, p, nitems);
-    else if (CS == 2) s = tc::launch_tc<256, 2, 1>(P, p, nitems);
-    else if (vpl == 2) s = tc::launch_tc<256, 1, 2>(P, p, nitems);
-    else s = tc::launch_tc<256, 1, 1>(P, p, nitems);
-  } else {
-    if (CS == 2) s = tc::launch_tc<128, 2, 1>(P, p, nitems);
-    else if (vpl == 2) s = tc::launch_tc<128, 1, 2>(P, p, nitems);
-    else s = tc::launch_tc<128, 1, 1>(P, p, nitems);
-  }
+  if (TN == 256)
+    s = pair ? tc::launch_tc<256, true>(P, p, nitems) : tc::launch_tc<256, false>(P, p, nitems);
+  else
+    s = tc::launch_tc<128, false>(P, p, nitems);
   if (s != GV_OK) return s;
   float* out = d_result + (mode == 0 ? (int64_t)(flag_opt % 2) * p.MN : 0);
   tc::k_reduce_partials<<<(unsigned)((p.MN + 255) / 256), 256, 0, P.stream>>>(

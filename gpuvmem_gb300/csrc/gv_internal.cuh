@@ -199,6 +199,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
                    int only_channel, int mode);
 bool dchi2_tc_supported(const Problem& P);
 int tc_tile_n(const Problem& P);
+bool tc_pair(const Problem& P);
 gv_status check_device_error(Problem& P);
 
 // optimiser

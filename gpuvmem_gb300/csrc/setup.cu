@@ -510,17 +510,20 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_LAUNCH("k_dirty_max");
   }
   // split-K partial images of the tensor-core engine: pick the split count
-  // that fills whole waves of SMs, keeping >= 1024 visibilities per item
+  // that fills whole waves of SMs (of CTA pairs in pair mode), keeping
+  // >= 1024 visibilities per item
   if (P.N >= 128) {
-    const int TN = P.N >= 256 ? 256 : 128;
-    const int64_t tiles = (int64_t)(P.N / 128) * (P.N / TN);
+    const int TN = tc_tile_n(P);
+    const bool pair = tc_pair(P);
+    const int64_t tiles = (int64_t)(P.N / 128) * (P.N / TN) / (pair ? 2 : 1);
+    const int64_t workers = std::max(1, pair ? P.num_sms / 2 : P.num_sms);
     int64_t nmax = std::max<int64_t>(1, P.Vgrid / 1024);
     int best = 1;
     double best_util = -1.0;
     for (int64_t s = 1; s <= std::min<int64_t>(nmax, 256); s++) {
       const int64_t items = tiles * s;
-      const int64_t waves = (items + P.num_sms - 1) / P.num_sms;
-      const double util = (double)items / (double)(waves * P.num_sms);
+      const int64_t waves = (items + workers - 1) / workers;
+      const double util = (double)items / (double)(waves * workers);
       if (util > best_util + 0.02) {
         best_util = util;
         best = (int)s;

@@ -80,3 +80,30 @@ def test_tc_alpha_plane():
         nud = np.float64(np.float32(data.freqs[c]) / np.float32(data.nu_0))
         mag += np.abs(orc.dchi2_channel(c) * img_c[0] * nud ** img_c[1] * orc.fg_scale * np.log(nud))
     assert np.abs(got - ref).max() <= GRAD_TOL * mag.max()
+
+
+@pytest.mark.parametrize("env", [{"GV_TC_PAIR": "0"}, {"GV_TC_SLAB": "1"},
+                                 {"GV_TC_ACCURATE_ANCHOR": "1"},
+                                 {"GV_TC_PAIR": "0", "GV_TC_SLAB": "3"}])
+def test_tc_launch_variants_match_simt(env, monkeypatch):
+    """CTA pairs (cta_group::2) and single CTAs, the drain period and the
+    anchor phasor's sin/cos give the same gradient as the exact SIMT engine."""
+    import torch
+    import gpuvmem_gb300 as gv
+    data, orc, _ = build(512, 3, 123, engine=1)
+    p1 = gv.Problem(data, TERMS, engine=1)
+    img = image(orc, 9)
+    d1 = torch.from_numpy(img.copy()).cuda()
+    p1.chi2(d1)
+    ref = p1.dchi2(d1).cpu().numpy()
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    p2 = gv.Problem(data, TERMS, engine=2)
+    d2 = torch.from_numpy(img.copy()).cuda()
+    p2.chi2(d2)
+    got = p2.dchi2(d2).cpu().numpy()
+    monkeypatch.undo()
+    got_default = p2.dchi2(d2).cpu().numpy()
+    scale = np.abs(ref[0]).max()
+    assert np.abs(got - ref).max() <= GRAD_TOL * scale
+    assert np.abs(got_default - ref).max() <= GRAD_TOL * scale
