@@ -38,10 +38,11 @@
 //   8 generator warps   wait for the chunk's visibility constants and a free
 //                       stage, generate, and arrive on the stage's "full"
 //                       barrier;
-//   4 drain warps       (one per TMEM lane quarter) drain the accumulator
-//                       halves into the running sum, and at the end of a
-//                       channel apply the epilogue factor (beam, fg_scale,
-//                       chain rule) and add it to this split's partial image;
+//   8 drain warps       (two per TMEM lane quarter, one column slice each)
+//                       drain the accumulator into the running sum, and at
+//                       the end of a channel apply the epilogue factor
+//                       (beam, fg_scale, chain rule) and add it to this
+//                       split's partial image;
 //   loader warp         loads the visibility constants of chunks up to five
 //                       ahead into a 6-slot ring (global loads issued two
 //                       chunks before they are needed);
@@ -75,9 +76,10 @@ constexpr int kTM = 128;            // image rows per CTA tile (MMA M per CTA)
 constexpr int kChunkVis = 32;       // visibilities per chunk
 constexpr int kKC = 2 * kChunkVis;  // K elements per chunk
 constexpr int kGW = 8;              // generator warps (two per scheduler)
-constexpr int kDW = 4;              // drain warps (one per TMEM lane quarter)
-// generator, drain, loader and MMA warps: 14 warps, at most 4 per scheduler,
-// so up to 128 registers a thread
+constexpr int kDW = 8;              // drain warps (two per TMEM lane quarter)
+constexpr int kDH = kDW / 4;        // drain warps per lane quarter (column slices)
+// generator, drain, loader and MMA warps: 18 warps, at most 5 per scheduler,
+// so up to 96 registers a thread
 constexpr int kThreads = (kGW + kDW + 2) * 32;
 constexpr int kVPL = 2;             // visibilities per generator lane (packed FP32x2 chains)
 constexpr int kVisSlots = 6;
@@ -183,7 +185,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, volatile
     if (mbar_try_wait_sleep(m, parity)) return true;
     if (*abort) return false;
     if (clock64() - t0 > kWaitCycles) {
-      atomicExch(err, code);
+      atomicCAS(err, 0u, code);  // keep the first cause
       *abort = 1;
       return false;
     }
@@ -297,6 +299,38 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 #pragma unroll
   for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
 }
+// 32 columns from TMEM without waiting; tmem_wait_ld64 completes two of them
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+}
+// wait for the TMEM loads in flight; the registers of both loads pass
+// through the statement so no use of them is scheduled before it
+__device__ __forceinline__ void tmem_wait_ld64(uint32_t* a, uint32_t* b) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]),
+                 "+r"(a[6]), "+r"(a[7]), "+r"(a[8]), "+r"(a[9]), "+r"(a[10]), "+r"(a[11]),
+                 "+r"(a[12]), "+r"(a[13]), "+r"(a[14]), "+r"(a[15]), "+r"(a[16]), "+r"(a[17]),
+                 "+r"(a[18]), "+r"(a[19]), "+r"(a[20]), "+r"(a[21]), "+r"(a[22]), "+r"(a[23]),
+                 "+r"(a[24]), "+r"(a[25]), "+r"(a[26]), "+r"(a[27]), "+r"(a[28]), "+r"(a[29]),
+                 "+r"(a[30]), "+r"(a[31]), "+r"(b[0]), "+r"(b[1]), "+r"(b[2]), "+r"(b[3]),
+                 "+r"(b[4]), "+r"(b[5]), "+r"(b[6]), "+r"(b[7]), "+r"(b[8]), "+r"(b[9]),
+                 "+r"(b[10]), "+r"(b[11]), "+r"(b[12]), "+r"(b[13]), "+r"(b[14]), "+r"(b[15]),
+                 "+r"(b[16]), "+r"(b[17]), "+r"(b[18]), "+r"(b[19]), "+r"(b[20]), "+r"(b[21]),
+                 "+r"(b[22]), "+r"(b[23]), "+r"(b[24]), "+r"(b[25]), "+r"(b[26]), "+r"(b[27]),
+                 "+r"(b[28]), "+r"(b[29]), "+r"(b[30]), "+r"(b[31])
+               :
+               : "memory");
+}
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
@@ -375,13 +409,14 @@ struct TcParams {
 };
 
 // Shared-memory layout of one CTA.  A: 128 rows; B: the TN columns of the
-// tile (single) or this CTA's TN/2 of them (pair).  B atom a of the CTA
-// belongs to accumulator half a / kHatoms.
-template <int TN, bool PAIR>
+// tile (single) or this CTA's TN/2 of them (pair).  The accumulator is
+// issued in NP parts of TN/NP columns; B atom a of the CTA belongs to part
+// a / kPatoms.
+template <int TN, bool PAIR, int NP>
 struct Layout {
   static constexpr int kBcols = PAIR ? TN / 2 : TN;
   static constexpr int kBatoms = kBcols / 64;
-  static constexpr int kHatoms = kBatoms / 2;            // B atoms per accumulator half
+  static constexpr int kPatoms = kBatoms / NP;           // B atoms per accumulator part
   static constexpr uint32_t kSboA = (kTM / 64) * 1024;   // bytes between K atoms of A
   static constexpr uint32_t kSboB = kBatoms * 1024;
   static constexpr uint32_t kTileA = kSboA * (kKC / 8);  // one A part (hi or lo)
@@ -558,12 +593,16 @@ __device__ __forceinline__ void drain_cols(uint32_t t_acc, uint32_t t_run, uint3
 #pragma unroll 1
   for (int cb = 0; cb < ncols; cb += 32) {
     const uint32_t col = (uint32_t)(col0 + cb);
-    float acc[32], run[32];
-    tmem_ld32(t_acc + lane_off + col, acc);
-    if (!run_empty) {
-      tmem_ld32(t_run + lane_off + col, run);
+    float acc[32];
+    if (run_empty) {
+      tmem_ld32(t_acc + lane_off + col, acc);
+    } else {
+      uint32_t ra[32], rr[32];
+      tmem_ld32_nowait(t_acc + lane_off + col, ra);
+      tmem_ld32_nowait(t_run + lane_off + col, rr);
+      tmem_wait_ld64(ra, rr);
 #pragma unroll
-      for (int k = 0; k < 32; k++) acc[k] += run[k];
+      for (int k = 0; k < 32; k++) acc[k] = __uint_as_float(ra[k]) + __uint_as_float(rr[k]);
     }
     tmem_st32(t_run + lane_off + col, acc);
   }
@@ -618,11 +657,11 @@ __device__ __forceinline__ void iter_next(const TcParams& p, int nitems, int str
   iter_seek(p, nitems, stride, it);
 }
 
-template <int TN, bool PAIR>
+template <int TN, bool PAIR, int NP>
 __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
-  using L = Layout<TN, PAIR>;
+  using L = Layout<TN, PAIR, NP>;
   constexpr int S = L::kStages;
-  constexpr int NH = TN / 2;  // accumulator columns per half
+  constexpr int NH = TN / NP;  // accumulator columns per part
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -632,7 +671,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   uint64_t* op_empty = bars + 3;   // [S]  one MMA commit
   uint64_t* vis_full = bars + 6;   // [6]  32 arrives (control lanes)
   uint64_t* vis_empty = bars + 12; // [6]  one arrive per generator warp
-  uint64_t* acc0_done = bars + 18; // [1]  MMA commit after the first accumulator half
+  uint64_t* acc0_done = bars + 18; // [1]  MMA commit after part 0 of a drain chunk
   uint64_t* drained = bars + 19;   // [2]  one arrive per drain warp of the pair (leader)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 24);
   __shared__ int s_abort;
@@ -659,8 +698,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
       mbar_init(&vis_empty[s], kGW);
     }
     mbar_init(acc0_done, 1);
-    mbar_init(&drained[0], kDW * peers);
-    mbar_init(&drained[1], kDW * peers);
+    for (int h = 0; h < NP; h++) mbar_init(&drained[h], kDW * peers);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -787,13 +825,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         } else {
           const uint32_t lw = lo0 + (uint32_t)st * (L::kStage >> 4);
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
+          for (int h = 0; h < NP; h++) {
             if (fresh && nch > 0) ok = mbar_wait(&drained[h], (ndrain - 1) & 1, abort, p.err, 6u);
             if (!ok) break;
             fence_after();
             const uint32_t d = t_acc + (uint32_t)(h * NH);
             constexpr uint32_t kB = 2 * L::kTileA;
-            const uint32_t boff = (uint32_t)(h * L::kHatoms * 1024);
+            const uint32_t boff = (uint32_t)(h * L::kPatoms * 1024);
 #pragma unroll
             for (int t = 0; t < kKC / 16; t++) {
               const uint64_t ah = desc(lw + ((t * 2 * L::kSboA) >> 4), hiA);
@@ -818,7 +856,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         const long long t0 = clock64();
         while (!mbar_try_wait(&op_empty[q % S], (q / S) & 1)) {
           if (clock64() - t0 > kWaitCycles) {
-            atomicExch(p.err, 7u);
+            atomicCAS(p.err, 0u, 7u);
             break;
           }
         }
@@ -828,6 +866,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
     // ------------------------------- drain warps ---------------------------
     const int lq = warp & 3;
     const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
+    // column slice of this warp within each accumulator part and the tile
+    constexpr int kSliceP = NH / kDH, kSliceT = TN / kDH;
+    const int dq = (warp - kGW) >> 2;
     uint32_t ndr = 0;
     bool ok = true;
     for (int item = cid; item < nitems && ok; item += ncl) {
@@ -850,26 +891,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           const uint32_t my = nch++;
           const bool last = (n == nchunks - 1);
           if (!last && (n % p.slab) != p.slab - 1) continue;
-          // first half: its MMAs are committed before the second half's
+          // An mbarrier wait on parity only tells the phase apart from its
+          // neighbours, so a waiter must not get ahead of the barrier by a
+          // phase.  acc0_done completes once per drain chunk (after part 0),
+          // and this warp waits for its phases in order.  The chunk's
+          // op_empty phase (last part of two) is waited for only after
+          // acc0_done showed the tensor core reached this chunk.
           ok = warp_wait(acc0_done, ndr & 1, abort, p.err, 3u);
           if (!ok) break;
           fence_after();
-          drain_cols(t_acc, t_run, lane_off, 0, NH, run_empty);
+          drain_cols(t_acc, t_run, lane_off, dq * kSliceP, kSliceP, run_empty);
           fence_before();
           warp_arrive_leader<PAIR>(&drained[0]);
-          // second half: the chunk's final commit
-          ok = warp_wait(&op_empty[my % S], (my / S) & 1, abort, p.err, 8u);
-          if (!ok) break;
-          fence_after();
-          drain_cols(t_acc, t_run, lane_off, NH, NH, run_empty);
-          fence_before();
-          warp_arrive_leader<PAIR>(&drained[1]);
+          if (NP == 2) {
+            ok = warp_wait(&op_empty[my % S], (my / S) & 1, abort, p.err, 8u);
+            if (!ok) break;
+            fence_after();
+            drain_cols(t_acc, t_run, lane_off, NH + dq * kSliceP, kSliceP, run_empty);
+            fence_before();
+            warp_arrive_leader<PAIR>(&drained[1]);
+          }
           ndr++;
           run_empty = false;
           if (last) {
             // channel epilogue: partial (+)= factor * running sum
 #pragma unroll 1
-            for (int cb = 0; cb < TN; cb += 32) {
+            for (int cb = dq * kSliceT; cb < (dq + 1) * kSliceT; cb += 32) {
               float run[32];
               tmem_ld32(t_run + lane_off + (uint32_t)cb, run);
 #pragma unroll 4
@@ -888,7 +935,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
       }
       if (ok && first_channel) {
         // no visibilities in this split for this tile: its partial is zero
-        for (int k = 0; k < TN; k++) prow[k] = 0.0f;
+        for (int k = dq * kSliceT; k < (dq + 1) * kSliceT; k++) prow[k] = 0.0f;
       }
     }
   } else {
@@ -939,8 +986,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
               const int batom = w2 / kVq;
               const int kv0 = (w2 % kVq) * 4 * kVPL + kq;
               // global column of this atom within the TN-wide tile
-              const int col = (batom / L::kHatoms) * NH + (PAIR ? (int)rank * (NH / 2) : 0) +
-                              (batom % L::kHatoms) * 64;
+              const int col = (batom / L::kPatoms) * NH + (PAIR ? (int)rank * (NH / 2) : 0) +
+                              (batom % L::kPatoms) * 64;
               const int r0 = j0 + col + oct * 8 - p.x0;
               gen_task<true, kFast>(b_hi, b_lo, L::kSboB, batom, r0, sv, kv0, oct);
             }
@@ -974,10 +1021,10 @@ __global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restric
   out[q] += (float)s;
 }
 
-template <int TN, bool PAIR>
+template <int TN, bool PAIR, int NP>
 gv_status launch_tc(const Problem& P, const TcParams& p, int nitems) {
-  auto kern = k_dchi2_tc<TN, PAIR>;
-  const size_t smem = Layout<TN, PAIR>::kSmem;
+  auto kern = k_dchi2_tc<TN, PAIR, NP>;
+  const size_t smem = Layout<TN, PAIR, NP>::kSmem;
   GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -1086,11 +1133,20 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.Ktot = P.Vgrid;
   }
   const int nitems = (p.ntile_i / (pair ? 2 : 1)) * p.ntile_j * p.nsplit;
+  // accumulator parts: 2 lets the first half drain while the tensor core
+  // works on the second; 1 issues full-width MMAs (less shared-memory
+  // traffic per product)
+  int np = 1;
+  if (const char* e = std::getenv("GV_TC_PARTS")) np = std::atoi(e) == 2 ? 2 : 1;
   gv_status s;
-  if (TN == 256)
-    s = pair ? tc::launch_tc<256, true>(P, p, nitems) : tc::launch_tc<256, false>(P, p, nitems);
-  else
-    s = tc::launch_tc<128, false>(P, p, nitems);
+  if (TN == 256) {
+    if (pair)
+      s = np == 2 ? tc::launch_tc<256, true, 2>(P, p, nitems) : tc::launch_tc<256, true, 1>(P, p, nitems);
+    else
+      s = np == 2 ? tc::launch_tc<256, false, 2>(P, p, nitems) : tc::launch_tc<256, false, 1>(P, p, nitems);
+  } else {
+    s = np == 2 ? tc::launch_tc<128, false, 2>(P, p, nitems) : tc::launch_tc<128, false, 1>(P, p, nitems);
+  }
   if (s != GV_OK) return s;
   float* out = d_result + (mode == 0 ? (int64_t)(flag_opt % 2) * p.MN : 0);
   tc::k_reduce_partials<<<(unsigned)((p.MN + 255) / 256), 256, 0, P.stream>>>(

@@ -83,11 +83,12 @@ def test_tc_alpha_plane():
 
 
 @pytest.mark.parametrize("env", [{"GV_TC_PAIR": "0"}, {"GV_TC_SLAB": "1"},
-                                 {"GV_TC_ACCURATE_ANCHOR": "1"},
-                                 {"GV_TC_PAIR": "0", "GV_TC_SLAB": "3"}])
+                                 {"GV_TC_ACCURATE_ANCHOR": "1"}, {"GV_TC_PARTS": "2"},
+                                 {"GV_TC_PAIR": "0", "GV_TC_PARTS": "2", "GV_TC_SLAB": "3"}])
 def test_tc_launch_variants_match_simt(env, monkeypatch):
-    """CTA pairs (cta_group::2) and single CTAs, the drain period and the
-    anchor phasor's sin/cos give the same gradient as the exact SIMT engine."""
+    """CTA pairs (cta_group::2) and single CTAs, one or two accumulator parts,
+    the drain period and the anchor phasor's sin/cos give the same gradient
+    as the exact SIMT engine."""
     import torch
     import gpuvmem_gb300 as gv
     data, orc, _ = build(512, 3, 123, engine=1)
