@@ -110,6 +110,8 @@ def lib():
         "gv_prior_gradient": [vp, i32, vp, vp],
         "gv_objective": [vp, vp, i32, f64p, f64p],
         "gv_gradient": [vp, vp, vp, i32, i32],
+        "gv_evaluate": [vp, vp, vp, i32, i32, f64p, f64p],
+        "gv_problem_set_graphs": [vp, i32],
         "gv_optimize": [vp, C.POINTER(OptDesc), vp, C.POINTER(OptReport)],
         "gv_dirty_image": [vp, vp],
         "gv_residuals": [vp, f32p],
@@ -257,6 +259,20 @@ class Problem:
             xi = self._img()
         check(lib().gv_gradient(self.h, _ptr(img), _ptr(xi), it, flag_opt))
         return xi
+
+    def evaluate(self, img, it, flag_opt=0, xi=None):
+        """objective() then gradient() in one call, replayed from a CUDA graph
+        after the first call with the same buffers; returns (f, fi, xi)."""
+        if xi is None:
+            xi = self._img()
+        f = C.c_double()
+        fi = (C.c_double * 8)()
+        check(lib().gv_evaluate(self.h, _ptr(img), _ptr(xi), it, flag_opt, C.byref(f), fi))
+        return f.value, list(fi)[:len(self.terms)], xi
+
+    def set_graphs(self, enable: bool):
+        """Replay the optimiser's objective evaluations from CUDA graphs."""
+        check(lib().gv_problem_set_graphs(self.h, int(bool(enable))))
 
     def optimize(self, img, method="CG-FRPRMN", iterations=10, ftol=1e-12, gtol=1e-12, K=100,
                  flag=0, positivity=True) -> OptReport:

@@ -22,6 +22,7 @@ static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -221,6 +222,34 @@ gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter, in
   gv_status s = gv::gradient_launch(P, d_img, d_xi, iter, flag_opt);
   if (s != GV_OK) return s;
   return gv::check_device_error(P);
+}
+
+gv_status gv_evaluate(gv_problem* p, float* d_img, float* d_xi, int32_t iter, int32_t flag_opt,
+                      double* f, double* fi_values) {
+  GV_CHECK_PROBLEM(p);
+  Problem& P = p->P;
+  if (!d_img || !d_xi || !f || iter < 0) {
+    gv::set_error("invalid evaluate arguments");
+    return GV_ERR_INVALID;
+  }
+  gv_status s = gv::eval_graph(P, d_img, d_xi, iter, flag_opt, 3, true);
+  if (s != GV_OK) return s;
+  s = gv::fetch_scalars(P, gv::kSlotTerm0 + (int)P.terms.size());
+  if (s != GV_OK) return s;
+  double tot = 0.0;
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    const double v = P.h_scal[gv::kSlotTerm0 + t];
+    if (fi_values) fi_values[t] = v;
+    tot += (double)P.terms[t].lambda * v;
+  }
+  *f = tot;
+  return gv::check_device_error(P);
+}
+
+gv_status gv_problem_set_graphs(gv_problem* p, int32_t enable) {
+  GV_CHECK_PROBLEM(p);
+  p->P.use_graphs = enable ? 1 : 0;
+  return GV_OK;
 }
 
 gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img, gv_opt_report* report) {

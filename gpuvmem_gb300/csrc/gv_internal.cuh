@@ -123,6 +123,8 @@ struct Problem {
   int tc_nsplit = 0;
   int tc_fast_anchor = 1;        // SFU anchor phasor (GV_TC_ACCURATE_ANCHOR=1 selects sincospif)
   int num_sms = 0;
+  int use_graphs = 1;            // optimizer evaluations replayed from CUDA graphs
+  void* graphs = nullptr;        // graph cache (graph.cu)
 };
 
 // error state
@@ -138,6 +140,7 @@ gv_status cuda_fail(cudaError_t e, const char* what);
 // Counts every kernel launch of the library (gv_launch_count) and turns a
 // launch error into a status.
 void count_launch();
+void add_launches(int64_t n);
 #define GV_LAUNCH(what)                                         \
   do {                                                          \
     ::gv::count_launch();                                       \
@@ -201,6 +204,11 @@ bool dchi2_tc_supported(const Problem& P);
 int tc_tile_n(const Problem& P);
 bool tc_pair(const Problem& P);
 gv_status check_device_error(Problem& P);
+
+// CUDA-graph replay (graph.cu); what: 1 objective, 3 objective + gradient
+gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt, int what,
+                     bool store);
+void graph_cache_free(Problem& P);
 
 // optimiser
 gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep);

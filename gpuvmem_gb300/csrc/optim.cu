@@ -287,7 +287,8 @@ class Solver {
 
   // ObjectiveFunction::calcFunction as float (the reference's return type)
   gv_status func(float* img, bool store_res, float* out) {
-    gv_status s = objective_launch(P_, img, o_.flag, store_res);
+    gv_status s = P_.use_graphs ? eval_graph(P_, img, nullptr, 0, o_.flag, 1, store_res)
+                                : objective_launch(P_, img, o_.flag, store_res);
     if (s != GV_OK) return s;
     s = fetch_scalars(P_, kSlotTerm0 + (int)P_.terms.size());
     if (s != GV_OK) return s;

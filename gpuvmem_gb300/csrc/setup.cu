@@ -187,6 +187,7 @@ void free_problem(Problem& P) {
   cudaFree(P.d_flags);
   cudaFree(P.tc_partial);
   if (P.h_scal) cudaFreeHost(P.h_scal);
+  graph_cache_free(P);
   P = Problem();
 }
 
@@ -533,6 +534,10 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     const char* acc = std::getenv("GV_TC_ACCURATE_ANCHOR");
     P.tc_fast_anchor = (acc && acc[0] == '1') ? 0 : 1;
     GV_CUDA(cudaMalloc(&P.tc_partial, sizeof(float) * (size_t)best * MN));
+  }
+  {
+    const char* g = std::getenv("GV_GRAPHS");
+    P.use_graphs = (g && g[0] == '0') ? 0 : 1;
   }
   P.part_stride = 4 * P.num_sms;
   const int nslots = C + kMaxTerms + 8;

@@ -195,6 +195,21 @@ typedef struct gv_opt_report {
 gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img,
                       gv_opt_report* report);
 
+/* ObjectiveFunction::calcFunction followed by calcGradient(iter) at the
+ * same image (no single counterpart in the reference: frprmn.cu:99-101 and
+ * lbfgs.cu:111-113 call the two back to back).  The kernel sequence is
+ * captured into a CUDA graph on the first call with a given (d_img, d_xi,
+ * flag_opt, prior gating) and replayed with one launch afterwards; the
+ * result equals gv_objective then gv_gradient bit for bit.  The first call
+ * per key must not happen while the problem's stream is being captured. */
+gv_status gv_evaluate(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
+                      int32_t flag_opt, double* f, double* fi_values);
+
+/* 1 (default, or GV_GRAPHS unset/not "0" at creation): the optimiser's
+ * objective evaluations are replayed from CUDA graphs; 0: launched kernel by
+ * kernel.  Results are identical either way. */
+gv_status gv_problem_set_graphs(gv_problem* p, int32_t enable);
+
 /* Dirty image: the DChi2 adjoint applied to w*Vo (no beam, no fg_scale):
  * d_out[M*N] = sum_c sum_k w Re(conj(Vo) e^{i phi}). */
 gv_status gv_dirty_image(gv_problem* p, float* d_out);
