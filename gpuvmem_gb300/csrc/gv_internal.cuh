@@ -137,6 +137,15 @@ gv_status cuda_fail(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return ::gv::cuda_fail(_e, #call); \
   } while (0)
 
+// propagate a non-OK status
+#ifndef GV_TRY
+#define GV_TRY(expr)                 \
+  do {                               \
+    gv_status _s = (expr);           \
+    if (_s != GV_OK) return _s;      \
+  } while (0)
+#endif
+
 // Counts every kernel launch of the library (gv_launch_count) and turns a
 // launch error into a status.
 void count_launch();

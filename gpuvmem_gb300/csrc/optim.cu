@@ -313,11 +313,6 @@ class Solver {
     return func(w_.xt, false, out);
   }
 
-#define GV_TRY(expr)                 \
-  do {                               \
-    gv_status _s = (expr);           \
-    if (_s != GV_OK) return _s;      \
-  } while (0)
 
   // Bracketing of a minimum along the line (golden-section steps with
   // parabolic extrapolation); constants of src/mnbrak.cu:35-37.

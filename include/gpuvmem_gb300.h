@@ -236,6 +236,51 @@ gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float*
                                 float noise_cut, int32_t n, float prior_value, float eta,
                                 float epsilon, double* d_value, void* stream);
 
+/* ---- Learned warm start (no counterpart in the reference) --------------
+ * A 2-D U-Net that maps the dirty image and the PSF to a warm-start image
+ * for the solver.  Every convolution (forward, backward data, backward
+ * weight) runs as a BF16 GEMM on the tensor cores with FP32 accumulation;
+ * parameters, gradients and Adam state are FP32.  Tensors are NCHW FP32
+ * device buffers.  Parameters are one flat vector, layer by layer (weights
+ * [Cout][Cin][k][k] then bias [Cout]): encoder levels 0..L-1 (two 3x3
+ * convolutions each, ReLU), decoder levels L-2..0 (two 3x3 convolutions on
+ * [upsampled deeper level, encoder skip], ReLU), then a linear 1x1 output
+ * convolution.  Down-sampling is 2x2 averaging, up-sampling nearest. */
+typedef struct gv_unet gv_unet;
+typedef struct gv_unet_desc {
+  int32_t height, width;     /* square, divisible by 2^(levels-1) */
+  int32_t in_channels;       /* e.g. 2: dirty image and PSF */
+  int32_t base_channels;     /* channels at level 0 (multiple of 8); doubles per level, <= 256 */
+  int32_t levels;
+  int32_t max_batch;
+  uint64_t seed;             /* He-normal initialisation */
+} gv_unet_desc;
+gv_status gv_unet_create(const gv_unet_desc* desc, gv_unet** out);
+gv_status gv_unet_destroy(gv_unet* net);
+gv_status gv_unet_set_stream(gv_unet* net, void* stream);
+gv_status gv_unet_num_params(const gv_unet* net, int64_t* count);
+gv_status gv_unet_get_params(gv_unet* net, float* d_out);      /* device, num_params floats */
+gv_status gv_unet_set_params(gv_unet* net, const float* d_in); /* also resets Adam */
+gv_status gv_unet_get_grads(gv_unet* net, float* d_out);       /* of the last loss_grad / step */
+/* d_in: batch x in_channels x H x W; d_out: batch x 1 x H x W */
+gv_status gv_unet_forward(gv_unet* net, const float* d_in, int32_t batch, float* d_out);
+/* mean squared error against d_target (batch x 1 x H x W) and its gradient */
+gv_status gv_unet_loss_grad(gv_unet* net, const float* d_in, const float* d_target,
+                            int32_t batch, double* loss);
+/* loss_grad followed by one Adam step (beta 0.9 / 0.999, eps 1e-8) */
+gv_status gv_unet_train_step(gv_unet* net, const float* d_in, const float* d_target,
+                             int32_t batch, float lr, double* loss);
+/* One convolution layer on the tensor cores (test and tool entry points):
+ * y = act(conv_ks(x, w) + bias) with zero padding ks/2, act = ReLU if relu;
+ * backward: dx = conv^T(dz, w), dw, db from x and dz (dz is the gradient at
+ * the pre-activation). */
+gv_status gv_conv2d_forward(const float* x, const float* w, const float* bias, float* y,
+                            int32_t B, int32_t Cin, int32_t Cout, int32_t H, int32_t W,
+                            int32_t ks, int32_t relu, void* stream);
+gv_status gv_conv2d_backward(const float* x, const float* w, const float* dz, float* dx,
+                             float* dw, float* db, int32_t B, int32_t Cin, int32_t Cout,
+                             int32_t H, int32_t W, int32_t ks, void* stream);
+
 const char* gv_last_error(void);
 const char* gv_version(void);
 /* Diagnostics (no counterpart in the reference): number of kernels the
