@@ -113,7 +113,10 @@ def lib():
         "gv_evaluate": [vp, vp, vp, i32, i32, f64p, f64p],
         "gv_problem_set_graphs": [vp, i32],
         "gv_optimize": [vp, C.POINTER(OptDesc), vp, C.POINTER(OptReport)],
+        "gv_optimize_until": [vp, C.POINTER(OptDesc), vp, f64, i32, C.POINTER(OptReport)],
+        "gv_set_iteration": [vp, i32],
         "gv_dirty_image": [vp, vp],
+        "gv_psf_image": [vp, vp],
         "gv_residuals": [vp, f32p],
     }
     for name, args in sig.items():
@@ -282,10 +285,30 @@ class Problem:
         check(lib().gv_optimize(self.h, C.byref(o), _ptr(img), C.byref(rep)))
         return rep
 
+    def optimize_until(self, img, f_target, method="CG-FRPRMN", iterations=10, ftol=1e-12,
+                       gtol=1e-12, K=100, flag=0, positivity=True,
+                       priors_from_start=False) -> OptReport:
+        """optimize(), also stopping once f <= f_target (exit_reason 4)."""
+        kind = OPT_IDS[method] if isinstance(method, str) else method
+        o = OptDesc(kind, iterations, ftol, gtol, K, flag, int(positivity))
+        rep = OptReport()
+        check(lib().gv_optimize_until(self.h, C.byref(o), _ptr(img), float(f_target),
+                                      int(bool(priors_from_start)), C.byref(rep)))
+        return rep
+
+    def set_iteration(self, it: int):
+        check(lib().gv_set_iteration(self.h, int(it)))
+
     def dirty_image(self):
         import torch
         out = torch.zeros((self.N, self.M), dtype=torch.float32, device="cuda")
         check(lib().gv_dirty_image(self.h, _ptr(out)))
+        return out
+
+    def psf_image(self):
+        import torch
+        out = torch.zeros((self.N, self.M), dtype=torch.float32, device="cuda")
+        check(lib().gv_psf_image(self.h, _ptr(out)))
         return out
 
     def residuals(self) -> np.ndarray:

@@ -260,11 +260,36 @@ gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img, gv_op
   return gv::check_device_error(p->P);
 }
 
+gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img, double f_target,
+                            int32_t priors_from_start, gv_opt_report* report) {
+  GV_CHECK_PROBLEM(p);
+  if (!opt || !d_img) { gv::set_error("null optimizer descriptor or image"); return GV_ERR_INVALID; }
+  gv_status s = gv::optimize(p->P, *opt, d_img, report, f_target, priors_from_start ? 1 : 0);
+  if (s != GV_OK) return s;
+  return gv::check_device_error(p->P);
+}
+
+gv_status gv_set_iteration(gv_problem* p, int32_t iter) {
+  GV_CHECK_PROBLEM(p);
+  if (iter < 0) { gv::set_error("negative iteration"); return GV_ERR_INVALID; }
+  p->P.iteration = iter;
+  return GV_OK;
+}
+
 gv_status gv_dirty_image(gv_problem* p, float* d_out) {
   GV_CHECK_PROBLEM(p);
   Problem& P = p->P;
   if (!d_out) { gv::set_error("null output"); return GV_ERR_INVALID; }
   gv_status s = gv::dirty_launch(P, d_out);
+  if (s != GV_OK) return s;
+  return gv::check_device_error(P);
+}
+
+gv_status gv_psf_image(gv_problem* p, float* d_out) {
+  GV_CHECK_PROBLEM(p);
+  Problem& P = p->P;
+  if (!d_out) { gv::set_error("null output"); return GV_ERR_INVALID; }
+  gv_status s = gv::dirty_launch(P, d_out, true);
   if (s != GV_OK) return s;
   return gv::check_device_error(P);
 }

@@ -31,7 +31,7 @@ struct DirectParams {
   int normalize;
   int flag_opt;
   int c_begin, c_end;
-  int mode;  // 0 gradient (chain rule, 2 planes), 1 raw channel, 2 dirty image
+  int mode;  // 0 gradient (chain rule, 2 planes), 1 raw channel, 2 dirty image, 3 PSF
 };
 
 template <bool kDirty>
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256) k_dchi2_direct(
         s_w[t] = wl[g];
         if (kDirty) {
           const float4 d = deg[g];
-          const float2 o = vo[g];
+          const float2 o = dp.mode == 3 ? make_float2(1.0f, 0.0f) : vo[g];
           s_c[t] = make_float2(d.w * o.x, d.w * o.y);
         } else {
           s_c[t] = cvr[g];
@@ -159,7 +159,7 @@ gv_status dchi2_direct(Problem& P, const float* d_img, int flag_opt, float* d_re
   dp.c_end = only_channel >= 0 ? only_channel + 1 : (int)P.chans.size();
   dp.mode = mode;
   dim3 block(16, 16), grid((P.M + 15) / 16, (P.N + 15) / 16);
-  if (mode == 2) {
+  if (mode >= 2) {
     k_dchi2_direct<true><<<grid, block, 0, P.stream>>>(
         dp, P.d_chfreq, P.d_ranges, P.d_chnvis, P.d_ph, P.d_wl, P.d_cvr, P.d_deg, P.d_vo,
         P.d_mask, P.d_rho, d_img, d_result);

@@ -151,9 +151,10 @@ struct Layout {
 };
 
 // Epilogue factor of one pixel for channel c (mode 0: gradient with chain
-// rule; 1: raw channel DChi2; 2: dirty image), divided by the operand scale.
+// rule; 1: raw channel DChi2; 2: dirty image; 3: PSF), divided by the
+// operand scale.
 __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int j, float inv_s) {
-  if (p.mode == 2) return inv_s;
+  if (p.mode >= 2) return inv_s;
   const int64_t q = (int64_t)p.N * i + j;
   if (!(p.mask[q] & kMaskIn)) return 0.0f;
   const float freq = p.chfreq[c];
@@ -464,6 +465,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         if (p.mode == 2) {
           r.d = p.deg[g];
           r.r = p.vo[g];
+        } else if (p.mode == 3) {
+          r.d = p.deg[g];
+          r.r = make_float2(1.0f, 0.0f);
         } else {
           r.r = p.cvr[g];
         }
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         break;
       VisEntry ve;
       if (ra.valid) {
-        const float2 cc = p.mode == 2 ? make_float2(ra.d.w * ra.r.x, ra.d.w * ra.r.y) : ra.r;
+        const float2 cc = p.mode >= 2 ? make_float2(ra.d.w * ra.r.x, ra.d.w * ra.r.y) : ra.r;
         ve.FU = ra.ph.x;
         ve.FV = ra.ph.y;
         ve.GU = __uint_as_float(ra.ph.z);
@@ -841,7 +845,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
   p.img = d_img;
   p.partial = P.tc_partial;
   p.err = P.d_flags + kFlagErr;
-  p.cmax_bits = P.d_flags + (mode == 2 ? kFlagDirtyMax : kFlagCvrMax);
+  p.cmax_bits = P.d_flags + (mode == 2 ? kFlagDirtyMax : (mode == 3 ? kFlagPsfMax : kFlagCvrMax));
   if (only_channel >= 0) {
     p.C = 1;
     p.kc_off = P.d_kc_one + 2 * only_channel;

@@ -40,6 +40,7 @@ enum FlagSlot {
   kFlagCvrMax = 0,    // max |w Vr| component of the last stored residuals (float bits)
   kFlagDirtyMax = 1,  // max |w Vo| component (float bits)
   kFlagErr = 2,       // non-zero: a kernel gave up on a bounded wait
+  kFlagPsfMax = 3,    // max weight of a kept visibility (float bits)
   kNumFlags = 8
 };
 
@@ -202,7 +203,7 @@ gv_status fetch_scalars(Problem& P, int n);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);
 gv_status gradient_launch(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt);
-gv_status dirty_launch(Problem& P, float* d_out);
+gv_status dirty_launch(Problem& P, float* d_out, bool psf = false);
 
 // dchi2 engines
 gv_status dchi2_direct(Problem& P, const float* d_img, int flag_opt, float* d_result,
@@ -220,6 +221,7 @@ gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_o
 void graph_cache_free(Problem& P);
 
 // optimiser
-gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep);
+gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep,
+                   double f_target = -1e300, int first_iter = 0);
 
 }  // namespace gv

@@ -507,10 +507,12 @@ gv_status dchi2_channel_launch(Problem& P, int c, float* d_out) {
   return dchi2_direct(P, nullptr, 0, d_out, c, 1);
 }
 
-gv_status dirty_launch(Problem& P, float* d_out) {
+// dirty image (w Vo) or PSF (w), mode 2 / 3 of the DChi2 engines
+gv_status dirty_launch(Problem& P, float* d_out, bool psf) {
   GV_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * P.M * P.N, P.stream));
-  if (P.engine == 2) return dchi2_tc(P, nullptr, 0, d_out, -1, 2);
-  return dchi2_direct(P, nullptr, 0, d_out, -1, 2);
+  const int mode = psf ? 3 : 2;
+  if (P.engine == 2) return dchi2_tc(P, nullptr, 0, d_out, -1, mode);
+  return dchi2_direct(P, nullptr, 0, d_out, -1, mode);
 }
 
 // ObjectiveFunction::calcGradient (include/classes/objectivefunction.cuh:28-57)

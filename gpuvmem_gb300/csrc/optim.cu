@@ -475,12 +475,16 @@ class Solver {
     const int64_t PMN = 2 * MN_;
     float fp, fret = 0.0f;
     GV_TRY(func(img, true, &fp));
-    GV_TRY(grad(img, w_.xi, 0));
+    GV_TRY(grad(img, w_.xi, first_iter_));
     k_cg_init<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, w_.g, w_.xi, w_.h);
     GV_LAUNCH("k_cg_init");
     for (int it = 1; it <= o_.total_iterations; it++) {
       rep->iterations = it;
       GV_TRY(linmin(img, w_.xi, &fret));
+      if (it >= 2 && (double)fret <= f_target_) {
+        rep->exit_reason = 4;
+        break;
+      }
       if (2.0f * std::fabs(fret - fp) <= o_.ftol * (std::fabs(fret) + std::fabs(fp) + 1.0e-10)) {
         rep->exit_reason = 1;
         break;
@@ -519,7 +523,7 @@ class Solver {
     float fp, fret = 0.0f;
     std::vector<float> alpha(2 * (size_t)K);
     GV_TRY(func(img, true, &fp));
-    GV_TRY(grad(img, w_.xi, 0));
+    GV_TRY(grad(img, w_.xi, first_iter_));
     k_scale<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, -1.0f, w_.xi);
     GV_LAUNCH("k_scale");
     auto slot = [&](float* base, int im, int k) { return base + MN_ * im * k + MN_ * im; };
@@ -529,6 +533,10 @@ class Solver {
       GV_CUDA(cudaMemcpyAsync(w_.p_old, img, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
       GV_CUDA(cudaMemcpyAsync(w_.xi_old, w_.xi, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
       GV_TRY(linmin(img, w_.xi, &fret));
+      if (it >= 2 && (double)fret <= f_target_) {
+        rep->exit_reason = 4;
+        break;
+      }
       if ((fp - fret) / std::max({std::fabs(fret), std::fabs(fp), 1.0f}) <= o_.ftol) {
         rep->exit_reason = 1;
         break;
@@ -596,6 +604,12 @@ class Solver {
   }
 
   int64_t n_obj_ = 0, n_grad_ = 0;
+  // stop once a line search reaches this value (priors active, i.e. from
+  // the second iteration on); -inf: never
+  double f_target_ = -INFINITY;
+  // iteration number of the first gradient: 0 as the reference (priors off
+  // during the first line search), 1 to have them count from the start
+  int first_iter_ = 0;
 
  private:
   Problem& P_;
@@ -610,7 +624,8 @@ class Solver {
 
 }  // namespace
 
-gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep) {
+gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep,
+                   double f_target, int first_iter) {
   if (o.kind != GV_OPT_FRPRMN && o.kind != GV_OPT_LBFGS) {
     set_error("unknown optimizer kind");
     return GV_ERR_INVALID;
@@ -623,6 +638,8 @@ gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report
   std::memset(&r, 0, sizeof(r));
   const auto t0 = std::chrono::steady_clock::now();
   Solver s(P, o);
+  s.f_target_ = f_target;
+  s.first_iter_ = first_iter > 0 ? 1 : 0;
   gv_status st = s.init();
   if (st == GV_OK) st = o.kind == GV_OPT_FRPRMN ? s.frprmn(d_img, &r) : s.lbfgs(d_img, &r);
   if (st == GV_OK) {

@@ -105,17 +105,24 @@ __global__ void k_gather(int64_t n, const int64_t* __restrict__ idx,
   if (k < n) out[k] = in[idx[k]];
 }
 
+// max |w Vo| component (dirty image scale) and max w (PSF scale)
 __global__ void k_dirty_max(int64_t V, const float4* __restrict__ deg,
-                            const float2* __restrict__ vo, uint32_t* __restrict__ out) {
+                            const float2* __restrict__ vo, uint32_t* __restrict__ out,
+                            uint32_t* __restrict__ out_w) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float m = 0.0f;
+  float m = 0.0f, mw = 0.0f;
   if (k < V) {
     const float4 d = deg[k];
     const float2 o = vo[k];
     m = fmaxf(fabsf(d.w * o.x), fabsf(d.w * o.y));
+    mw = fabsf(d.w);
   }
-  for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, s));
+  for (int s = 16; s > 0; s >>= 1) {
+    m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, s));
+    mw = fmaxf(mw, __shfl_down_sync(0xffffffffu, mw, s));
+  }
   if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(out, __float_as_uint(m));
+  if ((threadIdx.x & 31) == 0 && mw > 0.0f) atomicMax(out_w, __float_as_uint(mw));
 }
 
 __global__ void k_weight_image(int M, int N, float xobs, float yobs, double DELTAX,
@@ -507,7 +514,8 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
   GV_CUDA(cudaMemsetAsync(P.d_flags, 0, sizeof(uint32_t) * kNumFlags, st));
   {
     const unsigned gb = (unsigned)((V + 255) / 256);
-    k_dirty_max<<<gb, 256, 0, st>>>(V, P.d_deg, P.d_vo, P.d_flags + kFlagDirtyMax);
+    k_dirty_max<<<gb, 256, 0, st>>>(V, P.d_deg, P.d_vo, P.d_flags + kFlagDirtyMax,
+                                    P.d_flags + kFlagPsfMax);
     GV_LAUNCH("k_dirty_max");
   }
   // split-K partial images of the tensor-core engine: pick the split count

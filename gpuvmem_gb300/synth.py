@@ -54,6 +54,7 @@ class SynthConfig:
     flag_fraction_range: tuple = (0.0, 0.0)
     alpha_range: Optional[tuple] = None
     seed: int = 0
+    array_seed: Optional[int] = None  # antenna layout seed (default: seed)
 
 
 CONFIG0 = SynthConfig(
@@ -249,7 +250,7 @@ def generate(cfg: SynthConfig, device: Optional[str] = None) -> SynthData:
     """Build the synthetic data set.  ``device`` = a torch CUDA device
     evaluates the sky visibilities there (large configurations); the default
     evaluates them with numpy."""
-    rng_array = np.random.default_rng([cfg.seed, 1])
+    rng_array = np.random.default_rng([cfg.seed if cfg.array_seed is None else cfg.array_seed, 1])
     rng_sky = np.random.default_rng([cfg.seed, 2])
     rng_noise = np.random.default_rng([cfg.seed, 3])
     rng_flag = np.random.default_rng([cfg.seed, 4])

@@ -210,9 +210,30 @@ gv_status gv_evaluate(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
  * kernel.  Results are identical either way. */
 gv_status gv_problem_set_graphs(gv_problem* p, int32_t enable);
 
+/* gv_optimize that also stops (exit_reason 4) once a line search from the
+ * second iteration on reaches f <= f_target (no counterpart in the
+ * reference: used to time convergence to a given objective).  With
+ * priors_from_start = 0 the priors are off during the first line search, as
+ * in the reference (Fi::iteration is 0 until the first calcGradient);
+ * with 1 the first gradient is taken as iteration 1, so they count from the
+ * start (used for warm starts, which are already near the solution). */
+gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img,
+                            double f_target, int32_t priors_from_start,
+                            gv_opt_report* report);
+
+/* Fi::setIteration(iter) on every term: iter > 0 makes the priors count in
+ * the next gv_objective (the reference sets it only inside calcGradient,
+ * include/classes/objectivefunction.cuh:39). */
+gv_status gv_set_iteration(gv_problem* p, int32_t iter);
+
 /* Dirty image: the DChi2 adjoint applied to w*Vo (no beam, no fg_scale):
  * d_out[M*N] = sum_c sum_k w Re(conj(Vo) e^{i phi}). */
 gv_status gv_dirty_image(gv_problem* p, float* d_out);
+
+/* Point-spread function: the same adjoint applied to w (Vr := 1), i.e. the
+ * dirty image of a 1 Jy point source at the phase centre (no counterpart in
+ * the reference; input of the warm-start network). */
+gv_status gv_psf_image(gv_problem* p, float* d_out);
 
 /* Copies the weighted residuals w*(Vo-Vm) of the last gv_chi2, in the
  * caller's visibility order, to a host buffer of 2*nvis_total floats. */

@@ -17,7 +17,8 @@ def _bf16_exact(rng, shape, scale=1.0):
 
 @pytest.mark.parametrize("B,Cin,Cout,H,ks,relu", [(2, 2, 32, 16, 3, True), (1, 96, 32, 12, 3, False),
                                                   (2, 32, 1, 16, 1, False), (1, 64, 128, 8, 3, True),
-                                                  (1, 256, 256, 8, 3, True), (3, 8, 64, 5, 3, False)])
+                                                  (1, 256, 256, 8, 3, True), (3, 8, 64, 5, 3, False),
+                                                  (1, 384, 128, 8, 3, True), (1, 24, 320, 6, 3, False)])
 def test_conv_forward_and_backward_match_oracle(B, Cin, Cout, H, ks, relu):
     import torch
     from gpuvmem_gb300 import unet

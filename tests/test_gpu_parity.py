@@ -207,6 +207,27 @@ def test_dirty_image(pair64):
     assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
 
 
+def test_psf_image(pair64):
+    """PSF = the adjoint applied to the weights (Vr := 1): sum_k w_k cos(phase)."""
+    data, orc, prob = pair64
+    got = prob.psf_image().cpu().numpy()
+    orc.chi2(orc.initial_image())
+    x0, y0 = int(data.xobs), int(data.yobs)
+    jj, ii = np.meshgrid(np.arange(data.M), np.arange(data.N))
+    x = (jj - x0) * data.DELTAX * np.pi / 180.0
+    y = (ii - y0) * data.DELTAY * np.pi / 180.0
+    zm1 = np.sqrt(1.0 - x * x - y * y) - 1.0
+    ref = np.zeros((data.N, data.M))
+    for c in range(len(data.freqs)):
+        o, e = data.chan_off[c], data.chan_off[c + 1]
+        u, v, w = orc.uvw[o:e, 0], orc.uvw[o:e, 1], orc.uvw[o:e, 2]
+        wt = orc.weight[o:e].astype(np.float64)
+        ph = 2 * np.pi * (x[..., None] * u + y[..., None] * v + zm1[..., None] * w)
+        ref += (wt * np.cos(ph)).sum(-1)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+    assert abs(ref[y0, x0] - orc.weight.astype(np.float64).sum()) <= 1e-9 * ref[y0, x0]
+
+
 @pytest.mark.parametrize("method", ["frprmn", "lbfgs"])
 def test_optimizer_trajectory(method):
     """Image after a fixed number of iterations.  Brent's minimiser works on

@@ -64,6 +64,9 @@ def test_tc_matches_simt_channels_and_dirty():
     a = p1.dirty_image().cpu().numpy()
     b = p2.dirty_image().cpu().numpy()
     assert np.abs(a - b).max() <= 2 * GRAD_TOL * np.abs(a).max()
+    a = p1.psf_image().cpu().numpy()
+    b = p2.psf_image().cpu().numpy()
+    assert np.abs(a - b).max() <= 2 * GRAD_TOL * np.abs(a).max()
 
 
 def test_tc_alpha_plane():
