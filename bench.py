@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3])
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--case", default=None, help="run a profiling case instead of the bench")
@@ -59,7 +59,7 @@ def parse():
 
 
 def workload(cfg_id):
-    cfg = synth.CONFIG1 if cfg_id == 1 else synth.CONFIG0
+    cfg = {0: synth.CONFIG0, 1: synth.CONFIG1, 2: synth.CONFIG2}[cfg_id]
     terms = [("Chi2", 1.0), ("Entropy", 0.01), ("TotalSquaredVariation", 1e-4)]
     return cfg, terms
 
@@ -176,6 +176,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.config == 3:
+        raise SystemExit("--impl reference covers configurations 0-2")
     cfg, terms = workload(args.config)
     data = synth.generate(cfg, device=None if args.config == 0 else _gen_device())
     times = []
@@ -318,6 +320,90 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batch(args):
+    """Configuration 3: 64 independent problems (sides 128-512, 20k-500k
+    visibilities each); a step is one objective + gradient evaluation of
+    every problem, all of them in one CUDA-graph launch (gv_batch)."""
+    import torch
+    import gpuvmem_gb300 as gv
+    rank = int(os.environ.get("RANK", "0"))
+    cfgs, lams = synth.config3_problems()
+    probs, imgs, xis = [], [], []
+    flops, nvis = 0.0, 0
+    for c, lam in zip(cfgs, lams):
+        d = synth.generate(c, device="cuda")
+        p = gv.Problem(d, [gv.term("Chi2", 1.0), gv.term("Entropy", lam)])
+        probs.append(p)
+        img = p.initial_image()
+        imgs.append(img)
+        xis.append(torch.zeros_like(img))
+        flops += 4.0 * c.n * c.n * p.info.nvis_in_grid
+        nvis += d.nvis
+    batch = gv.Batch(probs)
+    n = len(probs)
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / steps
+
+    launches0 = gv.launch_count()
+    with Clocks() as clk:
+        t_graph = timed(lambda: batch.evaluate(imgs, xis, 1), args.steps)
+    launches = (gv.launch_count() - launches0) // (args.steps + args.warmup)
+    batch.set_graphs(False)
+    t_streams = timed(lambda: batch.evaluate(imgs, xis, 1), args.steps)
+    batch.set_graphs(True)
+
+    def one_by_one():
+        for p, i_, x_ in zip(probs, imgs, xis):
+            p.objective(i_)
+            p.gradient(i_, 1, xi=x_)
+    t_seq = timed(one_by_one, max(1, args.steps // 2))
+    # end to end: every image in from pinned host memory, every gradient out
+    h_imgs = [torch.empty(i_.shape, dtype=torch.float32).pin_memory() for i_ in imgs]
+    h_xis = [torch.empty(i_.shape, dtype=torch.float32).pin_memory() for i_ in imgs]
+    for h, i_ in zip(h_imgs, imgs):
+        h.copy_(i_.cpu())
+
+    def e2e_step():
+        for h, i_ in zip(h_imgs, imgs):
+            i_.copy_(h, non_blocking=True)
+        batch.evaluate(imgs, xis, 1)
+        for h, x_ in zip(h_xis, xis):
+            h.copy_(x_, non_blocking=True)
+    t_e2e = timed(e2e_step, args.steps)
+    if rank != 0:
+        return
+    peaks, src = measured_peaks()
+    peak = peaks["bf16_tflops"] / 3.0
+    bytes_img = sum(i_.numel() * 4 for i_ in imgs)
+    line = {
+        "metric": METRIC, "value": n / t_graph, "unit": "problem " + METRIC, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_graph,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (DChi2: fp16 hi/lo x3, fp32 acc)", "data": "synthetic (seeded)",
+        "config": {"workload": f"batch of {n} independent problems (sides 128/256/512, "
+                               f"{nvis} visibilities in total), one graph launch per step",
+                   "problems": n, "visibilities": int(nvis), "step": "objective + gradient of every problem"},
+        "e2e": {"value": n / t_e2e, "unit": "problem " + METRIC,
+                "h2d_bytes_per_step": int(bytes_img), "d2h_bytes_per_step": int(bytes_img)},
+        "roofline": {"bound": "tensor", "achieved": flops / t_graph / 1e12, "peak": peak,
+                     "unit": "TFLOP/s", "frac": flops / t_graph / 1e12 / peak, "traffic": None,
+                     "kernel": "whole batch step (DChi2 FLOP over the step time)",
+                     "peak_source": f"{src} dense bf16 burst / 3"},
+        "batch_ms": {"one_graph": 1e3 * t_graph, "streams_no_graph": 1e3 * t_streams,
+                     "one_problem_after_another": 1e3 * t_seq},
+        "clocks": clk.summary(0), "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_case(name, reps):
     """Small fixed workloads for profiling one kernel (used by the commands
     recorded in profiles/): `dchi2_2048_1ch` (configuration 1 reduced to one
@@ -351,6 +437,8 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == 3:
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -118,6 +118,10 @@ def lib():
         "gv_dirty_image": [vp, vp],
         "gv_psf_image": [vp, vp],
         "gv_residuals": [vp, f32p],
+        "gv_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
+        "gv_batch_destroy": [vp],
+        "gv_batch_set_graphs": [vp, i32],
+        "gv_batch_evaluate": [vp, C.POINTER(vp), C.POINTER(vp), i32, i32, f64p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -315,3 +319,35 @@ class Problem:
         out = np.zeros((int(self.info.nvis_total), 2), dtype=np.float32)
         check(lib().gv_residuals(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
+
+
+class Batch:
+    """gv_batch: one objective + gradient evaluation of several independent
+    problems in one CUDA-graph launch."""
+
+    def __init__(self, problems: Sequence["Problem"]):
+        self.problems = list(problems)
+        arr = (C.c_void_p * len(self.problems))(*[p.h for p in self.problems])
+        h = C.c_void_p()
+        check(lib().gv_batch_create(arr, len(self.problems), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            try:
+                lib().gv_batch_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    def set_graphs(self, enable: bool):
+        check(lib().gv_batch_set_graphs(self.h, int(bool(enable))))
+
+    def evaluate(self, imgs, xis, it, flag_opt=0):
+        n = len(self.problems)
+        ia = (C.c_void_p * n)(*[t.data_ptr() for t in imgs])
+        xa = (C.c_void_p * n)(*[t.data_ptr() for t in xis])
+        f = (C.c_double * n)()
+        check(lib().gv_batch_evaluate(self.h, ia, xa, it, flag_opt, f))
+        return list(f)

@@ -17,6 +17,10 @@ struct gv_problem {
 };
 
 namespace gv {
+Problem& problem_of(gv_problem* p) { return p->P; }
+}  // namespace gv
+
+namespace gv {
 
 static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};

@@ -68,6 +68,15 @@ CONFIG1 = SynthConfig(
     dec_deg=-30.0, ha_start_h=-2.0, ha_stop_h=2.0, dt_s=4.0, n_sources=200,
     point_source_jy=1.0, weighting="briggs", robust=0.0, seed=2)
 
+# 4 spectral windows x 16 channels, 85-115 GHz, per-channel flag fraction
+# U(0, 0.4), spectral indices U(-1, 3): the batched MFS workload
+CONFIG2 = SynthConfig(
+    name="mfs-1024-64ch", n=1024, cell_arcsec=0.05, n_ant=40, disk_radius_m=1000.0,
+    freqs_hz=[f for spw in range(4) for f in np.linspace(85e9 + spw * 7.5e9,
+                                                          85e9 + spw * 7.5e9 + 7.0e9, 16)],
+    dec_deg=-30.0, ha_start_h=-1.0, ha_stop_h=1.0, dt_s=10.0, n_sources=40,
+    pb_fwhm_arcsec=40.0, flag_fraction_range=(0.0, 0.4), alpha_range=(-1.0, 3.0), seed=22)
+
 
 def small_config(n=64, n_ant=8, n_times=40, nchan=1, seed=0, pb_fwhm_frac=0.45,
                  weighting="natural", n_sources=6) -> SynthConfig:
@@ -306,3 +315,28 @@ def generate(cfg: SynthConfig, device: Optional[str] = None) -> SynthData:
         pb_cutoff=float(pb_cutoff), primary_beam=1, freqs=freqs, chan_off=chan_off,
         uvw_m=np.ascontiguousarray(uvw_m), vo=np.ascontiguousarray(vo),
         weight=weight, sources=src)
+
+
+def config3_problems(count: int = 64, seed: int = 3):
+    """Configuration 3: `count` independent problems with image sides drawn
+    from {128, 256, 512}, visibility counts log-uniform in [20k, 500k], 10-40
+    antennas, one channel at U(100, 300) GHz, their own skies, and an entropy
+    factor log-uniform in [1e-3, 1e-1].  Returns (configs, entropy factors)."""
+    rng = np.random.default_rng([seed, 99])
+    cfgs, lams = [], []
+    for k in range(count):
+        n = int(rng.choice([128, 256, 512]))
+        nvis = float(np.exp(rng.uniform(math.log(20e3), math.log(500e3))))
+        n_ant = int(rng.integers(10, 41))
+        nbl = n_ant * (n_ant - 1) // 2
+        n_t = max(4, int(round(nvis / nbl)))
+        freq = float(rng.uniform(100e9, 300e9))
+        cell = 0.05 * 230e9 / freq
+        span = 4.0
+        cfgs.append(SynthConfig(
+            name=f"batch-{k}-{n}", n=n, cell_arcsec=cell, n_ant=n_ant,
+            disk_radius_m=500.0, freqs_hz=[freq], dec_deg=-30.0, ha_start_h=-span / 2,
+            ha_stop_h=span / 2, dt_s=span * 3600.0 / n_t, n_sources=int(rng.integers(5, 30)),
+            pb_fwhm_arcsec=0.45 * n * cell, seed=1000 + k, source_radius_frac=0.2))
+        lams.append(float(np.exp(rng.uniform(math.log(1e-3), math.log(1e-1)))))
+    return cfgs, lams

@@ -257,6 +257,22 @@ gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float*
                                 float noise_cut, int32_t n, float prior_value, float eta,
                                 float epsilon, double* d_value, void* stream);
 
+/* ---- Batches of independent problems (no counterpart in the reference,
+ * which runs problems one after another) ---------------------------------
+ * One objective + gradient evaluation of every problem of the batch
+ * (different sizes and visibility counts allowed) is captured into one CUDA
+ * graph with a branch per problem and replayed with one launch and one
+ * synchronisation.  f[i] is problem i's objective; each problem's stored
+ * residuals, prior gating and scalars end as after gv_objective +
+ * gv_gradient.  A problem must not be in two batches evaluated at once. */
+typedef struct gv_batch gv_batch;
+gv_status gv_batch_create(gv_problem* const* problems, int32_t n, gv_batch** out);
+gv_status gv_batch_destroy(gv_batch* b);
+/* 1 (default): one graph launch; 0: kernel by kernel, each problem on its own stream */
+gv_status gv_batch_set_graphs(gv_batch* b, int32_t enable);
+gv_status gv_batch_evaluate(gv_batch* b, float* const* d_imgs, float* const* d_xis,
+                            int32_t iter, int32_t flag_opt, double* f);
+
 /* ---- Learned warm start (no counterpart in the reference) --------------
  * A 2-D U-Net that maps the dirty image and the PSF to a warm-start image
  * for the solver.  Every convolution (forward, backward data, backward
