@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--case", default=None, help="run a profiling case instead of the bench")
+    ap.add_argument("--autotune", action="store_true",
+                    help="measure and keep the fastest launch shapes before timing")
     return ap.parse_args()
 
 
@@ -221,6 +223,10 @@ def run_ours(args):
     prob = gv.Problem(data, [gv.term(k, lam) for k, lam in terms], engine=args.engine)
     stream = torch.cuda.current_stream()
     prob.set_stream(stream.cuda_stream)
+    tune = None
+    if args.autotune:
+        r = prob.autotune()
+        tune = {f: getattr(r, f) for f, _ in r._fields_}
     info = prob.info
     img = prob.initial_image()
     xi = torch.zeros_like(img)
@@ -315,6 +321,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "engine": info.dchi2_engine,
     }
+    if tune is not None:
+        line["autotune"] = tune
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -73,6 +73,13 @@ class OptDesc(C.Structure):
                 ("positivity", C.c_int32)]
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("tc_pair", C.c_int32), ("tc_nsplit", C.c_int32), ("degrid_threads", C.c_int32),
+                ("degrid_blocks", C.c_int32), ("dchi2_ms_default", C.c_double),
+                ("dchi2_ms_tuned", C.c_double), ("chi2_ms_default", C.c_double),
+                ("chi2_ms_tuned", C.c_double), ("candidates", C.c_int32)]
+
+
 class OptReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("exit_reason", C.c_int32), ("f_final", C.c_float),
                 ("n_objective", C.c_int64), ("n_gradient", C.c_int64), ("seconds", C.c_double)]
@@ -118,6 +125,7 @@ def lib():
         "gv_dirty_image": [vp, vp],
         "gv_psf_image": [vp, vp],
         "gv_residuals": [vp, f32p],
+        "gv_autotune": [vp, C.POINTER(TuneReport)],
         "gv_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
         "gv_batch_destroy": [vp],
         "gv_batch_set_graphs": [vp, i32],
@@ -299,6 +307,12 @@ class Problem:
         check(lib().gv_optimize_until(self.h, C.byref(o), _ptr(img), float(f_target),
                                       int(bool(priors_from_start)), C.byref(rep)))
         return rep
+
+    def autotune(self) -> TuneReport:
+        """Measure and keep the fastest DChi2 and degridding launch shapes."""
+        r = TuneReport()
+        check(lib().gv_autotune(self.h, C.byref(r)))
+        return r
 
     def set_iteration(self, it: int):
         check(lib().gv_set_iteration(self.h, int(it)))

@@ -273,6 +273,16 @@ gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img,
   return gv::check_device_error(p->P);
 }
 
+gv_status gv_autotune(gv_problem* p, gv_tune_report* report) {
+  GV_CHECK_PROBLEM(p);
+  gv_tune_report r;
+  std::memset(&r, 0, sizeof(r));
+  gv_status s = gv::autotune(p->P, &r);
+  if (report) *report = r;
+  if (s != GV_OK) return s;
+  return gv::check_device_error(p->P);
+}
+
 gv_status gv_set_iteration(gv_problem* p, int32_t iter) {
   GV_CHECK_PROBLEM(p);
   if (iter < 0) { gv::set_error("negative iteration"); return GV_ERR_INVALID; }

@@ -794,6 +794,7 @@ int tc_tile_n(const Problem& P) { return P.N >= 256 ? 256 : 128; }
 // single CTAs
 bool tc_pair(const Problem& P) {
   if (P.N < 256) return false;
+  if (P.tc_pair_mode >= 0) return P.tc_pair_mode == 1;
   const char* e = std::getenv("GV_TC_PAIR");
   return !(e && e[0] == '0');
 }

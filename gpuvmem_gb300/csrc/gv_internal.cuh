@@ -125,6 +125,10 @@ struct Problem {
   int tc_fast_anchor = 1;        // SFU anchor phasor (GV_TC_ACCURATE_ANCHOR=1 selects sincospif)
   int num_sms = 0;
   int use_graphs = 1;            // optimizer evaluations replayed from CUDA graphs
+  int tc_pair_mode = -1;         // -1: GV_TC_PAIR / default, 0 single CTAs, 1 CTA pairs
+  size_t tc_partial_cap = 0;     // split-K partial images the buffer holds
+  int degrid_threads = 256;      // k_degrid block size
+  int degrid_blocks = 0;         // k_degrid blocks per channel cap (0: part_stride)
   void* graphs = nullptr;        // graph cache (graph.cu)
 };
 
@@ -221,6 +225,7 @@ gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_o
 void graph_cache_free(Problem& P);
 
 // optimiser
+gv_status autotune(Problem& P, gv_tune_report* rep);
 gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep,
                    double f_target = -1e300, int first_iter = 0);
 

@@ -402,11 +402,13 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
   const int C = (int)P.chans.size();
   int64_t maxg = 1;
   for (auto& ch : P.chans) maxg = std::max<int64_t>(maxg, ch.ngrid);
-  int nb = (int)std::min<int64_t>((maxg + 255) / 256, P.part_stride);
+  const int th = P.degrid_threads;
+  const int cap = P.degrid_blocks > 0 ? std::min(P.degrid_blocks, P.part_stride) : P.part_stride;
+  int nb = (int)std::min<int64_t>((maxg + th - 1) / th, cap);
   if (nb < 1) nb = 1;
   const int64_t MN = (int64_t)P.M * P.N;
   if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
-  k_degrid<<<dim3(nb, C), 256, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
+  k_degrid<<<dim3(nb, C), th, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
                                               P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride,
                                               P.d_flags + kFlagCvrMax);
   GV_LAUNCH("k_degrid");

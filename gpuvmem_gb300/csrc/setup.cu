@@ -542,6 +542,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     const char* acc = std::getenv("GV_TC_ACCURATE_ANCHOR");
     P.tc_fast_anchor = (acc && acc[0] == '1') ? 0 : 1;
     GV_CUDA(cudaMalloc(&P.tc_partial, sizeof(float) * (size_t)best * MN));
+    P.tc_partial_cap = (size_t)best;
   }
   {
     const char* g = std::getenv("GV_GRAPHS");

@@ -257,6 +257,24 @@ gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float*
                                 float noise_cut, int32_t n, float prior_value, float eta,
                                 float epsilon, double* d_value, void* stream);
 
+/* Autotuner (the reference takes its launch shapes from the -X/-Y/-V
+ * flags, src/main.cu; here they are measured): times the candidates of the
+ * tensor-core DChi2 launch (CTA pairs or single CTAs x split-K counts) and of
+ * the degridding launch (block size x blocks per channel) on this problem
+ * and keeps the fastest.  Results stay within the parity tolerances of the
+ * defaults (only reduction orders change).  Runs a few objective and DChi2
+ * evaluations; call it before capturing graphs. */
+typedef struct gv_tune_report {
+  int32_t tc_pair;         /* 1 CTA pairs, 0 single CTAs (-1: DChi2 not on tensor cores) */
+  int32_t tc_nsplit;
+  int32_t degrid_threads;
+  int32_t degrid_blocks;   /* per channel */
+  double dchi2_ms_default, dchi2_ms_tuned;
+  double chi2_ms_default, chi2_ms_tuned;
+  int32_t candidates;      /* launch configurations timed */
+} gv_tune_report;
+gv_status gv_autotune(gv_problem* p, gv_tune_report* report);
+
 /* ---- Batches of independent problems (no counterpart in the reference,
  * which runs problems one after another) ---------------------------------
  * One objective + gradient evaluation of every problem of the batch
