@@ -412,13 +412,44 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def weighting_inputs(cfg):
+    """uvw (metres) and natural weights of a configuration's visibilities,
+    channel by channel (no sky needed for the weighting schemes)."""
+    rng = np.random.default_rng([cfg.seed, 1])
+    base = synth.baseline_uvw(cfg, rng)
+    C = len(cfg.freqs_hz)
+    uvw = np.concatenate([base] * C, axis=0)
+    off = np.arange(C + 1, dtype=np.int64) * base.shape[0]
+    w = np.full(uvw.shape[0], np.float32(1.0 / cfg.sigma_jy ** 2), dtype=np.float32)
+    freqs = np.array(cfg.freqs_hz, dtype=np.float32)
+    return uvw, w, freqs, off
+
+
 def run_case(name, reps):
     """Small fixed workloads for profiling one kernel (used by the commands
     recorded in profiles/): `dchi2_2048_1ch` (configuration 1 reduced to one
-    channel at 230 GHz, natural weights, 16 s integrations) and `cfg0`."""
+    channel at 230 GHz, natural weights, 16 s integrations), `cfg0`, and
+    `weighting` (Uniform and Briggs weighting of configuration 1's 35.28M
+    visibilities on a 2048^2 grid)."""
     import dataclasses
     import torch
     import gpuvmem_gb300 as gv
+    if name == "weighting":
+        cfg = synth.CONFIG1
+        uvw, w, freqs, off = weighting_inputs(cfg)
+        dx = -cfg.cell_arcsec / 3600.0
+        out = {}
+        for scheme, robust in (("uniform", 0.0), ("briggs", 0.0)):
+            gv.apply_weighting(scheme, robust, cfg.n, cfg.n, dx, -dx, freqs, off, uvw, w)
+            t = []
+            for _ in range(max(1, reps)):
+                t0 = time.perf_counter()
+                gv.apply_weighting(scheme, robust, cfg.n, cfg.n, dx, -dx, freqs, off, uvw, w)
+                t.append(time.perf_counter() - t0)
+            out[scheme] = 1e3 * min(t)
+        print(json.dumps({"case": name, "visibilities": int(off[-1]), "grid": cfg.n,
+                          "ms_including_host_copies": out}))
+        return
     if name == "dchi2_2048_1ch":
         cfg = dataclasses.replace(synth.CONFIG1, freqs_hz=[230e9], weighting="natural", dt_s=16.0)
     elif name == "cfg0":

@@ -126,6 +126,9 @@ def lib():
         "gv_psf_image": [vp, vp],
         "gv_residuals": [vp, f32p],
         "gv_autotune": [vp, C.POINTER(TuneReport)],
+        "gv_error_images": [vp, vp, vp],
+        "gv_apply_weighting": [i32, f32, i32, i32, f64, f64, i32, C.POINTER(ChannelDesc),
+                               C.POINTER(C.c_void_p), vp],
         "gv_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
         "gv_batch_destroy": [vp],
         "gv_batch_set_graphs": [vp, i32],
@@ -308,6 +311,12 @@ class Problem:
                                       int(bool(priors_from_start)), C.byref(rep)))
         return rep
 
+    def error_images(self, img):
+        """calculateErrors: (2, N, M) error images of the solution img."""
+        out = self._img()
+        check(lib().gv_error_images(self.h, _ptr(img), _ptr(out)))
+        return out
+
     def autotune(self) -> TuneReport:
         """Measure and keep the fastest DChi2 and degridding launch shapes."""
         r = TuneReport()
@@ -365,3 +374,29 @@ class Batch:
         f = (C.c_double * n)()
         check(lib().gv_batch_evaluate(self.h, ia, xa, it, flag_opt, f))
         return list(f)
+
+
+WEIGHTING = {"natural": 0, "uniform": 1, "briggs": 2}
+
+
+def apply_weighting(scheme, robust, M, N, deltax_deg, deltay_deg, freqs, chan_off, uvw_m,
+                    weight) -> np.ndarray:
+    """WeightingScheme::apply ("Natural", "Uniform", "Briggs") on the GPU for
+    one field and one correlation; returns the new float32 weights."""
+    C_ = len(freqs)
+    uvw_m = np.ascontiguousarray(uvw_m, dtype=np.float64)
+    w_in = np.ascontiguousarray(weight, dtype=np.float32)
+    out = np.empty_like(w_in)
+    chans = (ChannelDesc * C_)()
+    outs = (C.c_void_p * C_)()
+    for c in range(C_):
+        o, e = int(chan_off[c]), int(chan_off[c + 1])
+        chans[c].freq_hz = float(np.float32(freqs[c]))
+        chans[c].nvis = e - o
+        chans[c].uvw = uvw_m[o:e].ctypes.data_as(C.POINTER(C.c_double))
+        chans[c].vo = None
+        chans[c].weight = w_in[o:e].ctypes.data_as(C.POINTER(C.c_float))
+        outs[c] = out[o:e].ctypes.data
+    check(lib().gv_apply_weighting(WEIGHTING[scheme], float(robust), int(M), int(N),
+                                   float(deltax_deg), float(deltay_deg), C_, chans, outs, None))
+    return out

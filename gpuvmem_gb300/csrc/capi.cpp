@@ -273,6 +273,14 @@ gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img,
   return gv::check_device_error(p->P);
 }
 
+gv_status gv_error_images(gv_problem* p, float* d_img, float* d_err) {
+  GV_CHECK_PROBLEM(p);
+  if (!d_img || !d_err) { gv::set_error("null image or output"); return GV_ERR_INVALID; }
+  gv_status s = gv::error_images(p->P, d_img, d_err);
+  if (s != GV_OK) return s;
+  return gv::check_device_error(p->P);
+}
+
 gv_status gv_autotune(gv_problem* p, gv_tune_report* report) {
   GV_CHECK_PROBLEM(p);
   gv_tune_report r;

@@ -31,7 +31,8 @@ struct DirectParams {
   int normalize;
   int flag_opt;
   int c_begin, c_end;
-  int mode;  // 0 gradient (chain rule, 2 planes), 1 raw channel, 2 dirty image, 3 PSF
+  int mode;  // 0 gradient (chain rule, 2 planes), 1 raw channel, 2 dirty image, 3 PSF,
+             // 4 error-map sum: Re(w Vr e^{+2 pi i (x u + y v)}), no w-term
 };
 
 template <bool kDirty>
@@ -53,8 +54,10 @@ __global__ void __launch_bounds__(256) k_dchi2_direct(
   const int64_t q = inside ? (int64_t)dp.N * i + j : 0;
   const bool active = inside && (kDirty || (mask[q] & kMaskIn));
   const int jj = j - dp.x0, ii = i - dp.y0;
-  const float jj2 = (float)jj * (float)jj, ii2 = (float)ii * (float)ii;
-  const float rho = inside ? rho_img[q] : 0.0f;
+  // the error maps' phase has no w-term
+  const bool wterm = dp.mode != 4;
+  const float jj2 = wterm ? (float)jj * (float)jj : 0.0f, ii2 = wterm ? (float)ii * (float)ii : 0.0f;
+  const float rho = (inside && wterm) ? rho_img[q] : 0.0f;
   float res0 = 0.0f, res1 = 0.0f;
   double dirty = 0.0;
   for (int c = dp.c_begin; c < dp.c_end; c++) {
@@ -68,7 +71,10 @@ __global__ void __launch_bounds__(256) k_dchi2_direct(
         const int64_t g = rg.off + k0 + t;
         s_ph[t] = ph[g];
         s_w[t] = wl[g];
-        if (kDirty) {
+        if (kDirty && dp.mode == 4) {
+          const float2 r = cvr[g];
+          s_c[t] = make_float2(r.x, -r.y);
+        } else if (kDirty) {
           const float4 d = deg[g];
           const float2 o = dp.mode == 3 ? make_float2(1.0f, 0.0f) : vo[g];
           s_c[t] = make_float2(d.w * o.x, d.w * o.y);

@@ -151,8 +151,8 @@ struct Layout {
 };
 
 // Epilogue factor of one pixel for channel c (mode 0: gradient with chain
-// rule; 1: raw channel DChi2; 2: dirty image; 3: PSF), divided by the
-// operand scale.
+// rule; 1: raw channel DChi2; 2: dirty image; 3: PSF; 4: the error maps'
+// sum Re(w Vr e^{+2 pi i (x u + y v)})), divided by the operand scale.
 __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int j, float inv_s) {
   if (p.mode >= 2) return inv_s;
   const int64_t q = (int64_t)p.N * i + j;
@@ -489,11 +489,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
         break;
       VisEntry ve;
       if (ra.valid) {
-        const float2 cc = p.mode >= 2 ? make_float2(ra.d.w * ra.r.x, ra.d.w * ra.r.y) : ra.r;
+        // mode 2/3: w Vo or w; 4: conj(w Vr) with no w-term (error maps); else w Vr
+        const float2 cc = (p.mode == 2 || p.mode == 3)
+                              ? make_float2(ra.d.w * ra.r.x, ra.d.w * ra.r.y)
+                              : (p.mode == 4 ? make_float2(ra.r.x, -ra.r.y) : ra.r);
         ve.FU = ra.ph.x;
         ve.FV = ra.ph.y;
-        ve.GU = __uint_as_float(ra.ph.z);
-        ve.GV = __uint_as_float(ra.ph.w);
+        ve.GU = p.mode == 4 ? 0.0f : __uint_as_float(ra.ph.z);
+        ve.GV = p.mode == 4 ? 0.0f : __uint_as_float(ra.ph.w);
         ve.Eu = make_float2(ra.E.x, ra.E.y);
         ve.Ev = make_float2(ra.E.z, ra.E.w);
         ve.c = make_float2(cc.x * scale, cc.y * scale);

@@ -226,6 +226,7 @@ void graph_cache_free(Problem& P);
 
 // optimiser
 gv_status autotune(Problem& P, gv_tune_report* rep);
+gv_status error_images(Problem& P, float* d_img, float* d_err);
 gv_status optimize(Problem& P, const gv_opt_desc& o, float* d_img, gv_opt_report* rep,
                    double f_target = -1e300, int first_iter = 0);
 

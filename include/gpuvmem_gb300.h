@@ -257,6 +257,31 @@ gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float*
                                 float noise_cut, int32_t n, float prior_value, float eta,
                                 float epsilon, double* d_value, void* stream);
 
+/* Error images of a solution: calculateErrors (src/functions.cu:4966-5041):
+ * d_err (2*M*N, device) = 1/sqrt of the I_nu0 and alpha noise sums of
+ * I_nu_0_Noise / alpha_Noise (:4076, :4113), 0 outside the mask.  Evaluates
+ * chi2 at d_img first (clipping it, as the reference's last evaluation did)
+ * to get the residuals. */
+gv_status gv_error_images(gv_problem* p, float* d_img, float* d_err);
+
+/* Visibility weighting on the GPU: NaturalWeightingScheme::apply
+ * (src/naturalweightingscheme.cu:9), UniformWeightingScheme::apply
+ * (src/uniformweightingscheme.cu:9) and BriggsWeightingScheme::apply
+ * (src/briggsweightingscheme.cu:30) for one field and one correlation,
+ * without a uv taper.  Reads the channels' host uvw (metres) and weights,
+ * writes the new weights to weights_out[c] (host, may alias the input).
+ * The result equals the reference's with one OpenMP thread bit for bit
+ * (the reference's own result with more threads depends on its schedule). */
+typedef enum gv_weighting_kind {
+  GV_WEIGHT_NATURAL = 0,  /* "Natural" */
+  GV_WEIGHT_UNIFORM = 1,  /* "Uniform" */
+  GV_WEIGHT_BRIGGS = 2    /* "Briggs", robust parameter */
+} gv_weighting_kind;
+gv_status gv_apply_weighting(int32_t scheme, float robust, int32_t M, int32_t N,
+                             double deltax_deg, double deltay_deg, int32_t nchannels,
+                             const gv_channel_desc* channels, float* const* weights_out,
+                             void* stream);
+
 /* Autotuner (the reference takes its launch shapes from the -X/-Y/-V
  * flags, src/main.cu; here they are measured): times the candidates of the
  * tensor-core DChi2 launch (CTA pairs or single CTAs x split-K counts) and of
