@@ -430,7 +430,8 @@ def run_case(name, reps):
     recorded in profiles/): `dchi2_2048_1ch` (configuration 1 reduced to one
     channel at 230 GHz, natural weights, 16 s integrations), `cfg0`, and
     `weighting` (Uniform and Briggs weighting of configuration 1's 35.28M
-    visibilities on a 2048^2 grid)."""
+    visibilities on a 2048^2 grid) and `gridding` (the same visibilities
+    gridded with the PillBox2D and 7 x 7 PSWF kernels)."""
     import dataclasses
     import torch
     import gpuvmem_gb300 as gv
@@ -449,6 +450,26 @@ def run_case(name, reps):
             out[scheme] = 1e3 * min(t)
         print(json.dumps({"case": name, "visibilities": int(off[-1]), "grid": cfg.n,
                           "ms_including_host_copies": out}))
+        return
+    if name == "gridding":
+        cfg = synth.CONFIG1
+        uvw, w, freqs, off = weighting_inputs(cfg)
+        rng = np.random.default_rng([cfg.seed, 2])
+        vo = rng.normal(0.0, 1.0, (uvw.shape[0], 2)).astype(np.float32)
+        dx = -cfg.cell_arcsec / 3600.0
+        out = {}
+        for kind in ("PillBox2D", "PSWF"):
+            table, sup, _ = gv.ckernel_build(kind, cfg.n, cfg.n, dx, -dx)
+            res = gv.grid_visibilities(table, sup, cfg.n, cfg.n, dx, -dx, freqs, off, uvw, vo, w)
+            t = []
+            for _ in range(max(1, reps)):
+                t0 = time.perf_counter()
+                gv.grid_visibilities(table, sup, cfg.n, cfg.n, dx, -dx, freqs, off, uvw, vo, w)
+                t.append(time.perf_counter() - t0)
+            out[kind] = {"ms_including_host_copies": 1e3 * min(t), "taps": int(table.size),
+                         "gridded_visibilities": int(res[0][-1])}
+        print(json.dumps({"case": name, "visibilities": int(off[-1]), "grid": cfg.n,
+                          "channels": len(freqs), "kernels": out}))
         return
     if name == "dchi2_2048_1ch":
         cfg = dataclasses.replace(synth.CONFIG1, freqs_hz=[230e9], weighting="natural", dt_s=16.0)

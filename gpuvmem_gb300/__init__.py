@@ -22,9 +22,11 @@ _LIB = None
 GV_OK = 0
 STATUS = {0: "GV_OK", 1: "GV_ERR_INVALID", 2: "GV_ERR_CUDA", 3: "GV_ERR_NOMEM",
           4: "GV_ERR_UNSUPPORTED", 5: "GV_ERR_DEVICE"}
-FI_CHI2, FI_ENTROPY, FI_TSV, FI_TV, FI_L1, FI_LAPLACIAN = range(6)
+FI_CHI2, FI_ENTROPY, FI_TSV, FI_TV, FI_L1, FI_LAPLACIAN, FI_GENTROPY, FI_GL1, FI_QUADRATIC = \
+    range(9)
 FI_IDS = {"Chi2": FI_CHI2, "Entropy": FI_ENTROPY, "TotalSquaredVariation": FI_TSV,
-          "TotalVariation": FI_TV, "L1-Norm": FI_L1, "Laplacian": FI_LAPLACIAN}
+          "TotalVariation": FI_TV, "L1-Norm": FI_L1, "Laplacian": FI_LAPLACIAN,
+          "GEntropy": FI_GENTROPY, "GL1Norm": FI_GL1, "Quadratic": FI_QUADRATIC}
 OPT_FRPRMN, OPT_LBFGS = 0, 1
 OPT_IDS = {"CG-FRPRMN": OPT_FRPRMN, "CG-LBFGS": OPT_LBFGS}
 
@@ -38,7 +40,8 @@ class GvError(RuntimeError):
 class FiDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("lam", C.c_float), ("image_index", C.c_int32),
                 ("image_to_add", C.c_int32), ("prior_value", C.c_float), ("eta", C.c_float),
-                ("epsilon", C.c_float)]
+                ("epsilon", C.c_float), ("prior_image", C.POINTER(C.c_float)),
+                ("normalization_factor", C.c_float), ("epsilon_b", C.c_float)]
 
 
 class ChannelDesc(C.Structure):
@@ -55,7 +58,18 @@ class ProblemDesc(C.Structure):
                 ("initial_value", C.c_float), ("threshold", C.c_float),
                 ("normalize", C.c_int32), ("nchannels", C.c_int32),
                 ("channels", C.POINTER(ChannelDesc)), ("nterms", C.c_int32),
-                ("terms", C.POINTER(FiDesc)), ("dchi2_engine", C.c_int32)]
+                ("terms", C.POINTER(FiDesc)), ("dchi2_engine", C.c_int32),
+                ("gcf", C.POINTER(C.c_float))]
+
+
+class CKernelDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("m", C.c_int32), ("n", C.c_int32), ("amp", C.c_float),
+                ("w", C.c_float), ("alpha", C.c_float), ("w2", C.c_float)]
+
+
+class GridKernel(C.Structure):
+    _fields_ = [("m", C.c_int32), ("n", C.c_int32), ("support_x", C.c_int32),
+                ("support_y", C.c_int32), ("values", C.POINTER(C.c_float))]
 
 
 class ProblemInfo(C.Structure):
@@ -129,6 +143,11 @@ def lib():
         "gv_error_images": [vp, vp, vp],
         "gv_apply_weighting": [i32, f32, i32, i32, f64, f64, i32, C.POINTER(ChannelDesc),
                                C.POINTER(C.c_void_p), vp],
+        "gv_ckernel_defaults": [i32, i32, i32, C.POINTER(CKernelDesc)],
+        "gv_ckernel_build": [C.POINTER(CKernelDesc), i32, i32, f64, f64, vp,
+                             C.POINTER(i32), C.POINTER(i32), vp, C.POINTER(i32)],
+        "gv_grid_visibilities": [C.POINTER(GridKernel), i32, i32, f64, f64, i32,
+                                 C.POINTER(ChannelDesc), C.POINTER(ChannelDesc), vp],
         "gv_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
         "gv_batch_destroy": [vp],
         "gv_batch_set_graphs": [vp, i32],
@@ -159,12 +178,34 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def term(kind, lam, image_index=0, image_to_add=0, prior_value=0.001, eta=-1.0, epsilon=1e-12):
-    """One ObjectiveFunction term, as Fi::configure + setPrior would set it."""
+def term(kind, lam, image_index=0, image_to_add=0, prior_value=0.001, eta=-1.0, epsilon=1e-12,
+         prior_image=None, normalization_factor=1.0, epsilon_b=1e-12):
+    """One ObjectiveFunction term, as Fi::configure + setPrior would set it;
+    GEntropy and GL1Norm take a prior image (M*N) and its normalisation
+    factor, GL1Norm also epsilon_b (epsilon is its epsilon_a)."""
     if isinstance(kind, str):
         kind = FI_IDS[kind]
-    return (int(kind), float(lam), int(image_index), int(image_to_add), float(prior_value),
-            float(eta), float(epsilon))
+    t = (int(kind), float(lam), int(image_index), int(image_to_add), float(prior_value),
+         float(eta), float(epsilon))
+    if prior_image is not None:
+        t += (np.ascontiguousarray(prior_image, dtype=np.float32).reshape(-1),
+              float(normalization_factor), float(epsilon_b))
+    return t
+
+
+def _fi_desc(t, keep):
+    """FiDesc of a term tuple (7 fields, or 10 with a prior image)."""
+    d = FiDesc(*t[:7])
+    if len(t) > 7:
+        img = np.ascontiguousarray(t[7], dtype=np.float32).reshape(-1)
+        keep.append(img)
+        d.prior_image = img.ctypes.data_as(C.POINTER(C.c_float))
+        d.normalization_factor = float(t[8])
+        d.epsilon_b = float(t[9])
+    else:
+        d.normalization_factor = 1.0
+        d.epsilon_b = 1e-12
+    return d
 
 
 class Problem:
@@ -172,7 +213,7 @@ class Problem:
 
     def __init__(self, data, terms: Sequence[tuple], eta=-1.0, initial_value=0.001,
                  noise_cut=10.0, threshold=0.0, normalize=False, engine=0, vis_noise=-1.0,
-                 stream=None):
+                 stream=None, gcf=None):
         L = lib()
         self.data = data
         self.M, self.N = data.M, data.N
@@ -191,12 +232,19 @@ class Problem:
                                    w.ctypes.data_as(C.POINTER(C.c_float)))
         tl = (FiDesc * max(1, len(terms)))()
         for i, t in enumerate(terms):
-            tl[i] = FiDesc(*t)
+            tl[i] = _fi_desc(t, self._keep)
         self.terms = [t for t in terms if t[1] != 0.0]
         desc = ProblemDesc(data.M, data.N, data.DELTAX, data.DELTAY, data.xobs, data.yobs,
                            data.nu_0, data.antenna_diameter, data.pb_factor, data.pb_cutoff,
                            data.primary_beam, vis_noise, noise_cut, eta, initial_value,
                            threshold, int(normalize), C_, chans, len(terms), tl, engine)
+        if gcf is not None:
+            # gridding correction function of gridded data (Chi2::setCKernel)
+            g = np.ascontiguousarray(gcf, dtype=np.float32).reshape(-1)
+            if g.size != self.M * self.N:
+                raise ValueError("gcf must have M*N values")
+            self._keep.append(g)
+            desc.gcf = g.ctypes.data_as(C.POINTER(C.c_float))
         h = C.c_void_p()
         check(L.gv_problem_create(C.byref(desc), C.byref(h)))
         self.h = h
@@ -400,3 +448,109 @@ def apply_weighting(scheme, robust, M, N, deltax_deg, deltay_deg, freqs, chan_of
     check(lib().gv_apply_weighting(WEIGHTING[scheme], float(robust), int(M), int(N),
                                    float(deltax_deg), float(deltay_deg), C_, chans, outs, None))
     return out
+
+
+CKERNELS = {"PillBox2D": 0, "Gaussian2D": 1, "Sinc2D": 2, "GaussianSinc2D": 3, "PSWF": 4,
+            "pillbox": 0, "gaussian": 1, "sinc": 2, "gaussian_sinc": 3, "pswf": 4}
+
+
+def ckernel_build(kind, M, N, deltax_deg, deltay_deg, m=None, n=None, **params):
+    """MFS::configure's kernel set-up for CKernel `kind` (the reference's
+    registration ids or their lower-case names): returns (table [m, n] f32,
+    (support_x, support_y), gcf [M, N] f32 or None).  m, n default to the
+    reference's constructors: PillBox2D() is 1 x 1, the others 7 x 7;
+    params override amp, w, alpha, w2."""
+    k = CKERNELS[kind]
+    if m is None:
+        m = n = 1 if k == 0 else 7
+    n = m if n is None else n
+    d = CKernelDesc()
+    check(lib().gv_ckernel_defaults(k, int(m), int(n), C.byref(d)))
+    for key, v in params.items():
+        setattr(d, key, float(v))
+    table = np.zeros((m, n), np.float32)
+    gcf = np.zeros((M, N), np.float32)
+    sx, sy, hg = C.c_int32(), C.c_int32(), C.c_int32()
+    check(lib().gv_ckernel_build(C.byref(d), int(M), int(N), float(deltax_deg),
+                                 float(deltay_deg), table.ctypes.data, C.byref(sx), C.byref(sy),
+                                 gcf.ctypes.data, C.byref(hg)))
+    return table, (sx.value, sy.value), (gcf if hg.value else None)
+
+
+def grid_visibilities(table, support, M, N, deltax_deg, deltay_deg, freqs, chan_off, uvw_m, vo,
+                      weight):
+    """do_gridding on the GPU: returns (chan_off, uvw_m [k, 3] f64, vo [k, 2]
+    f32, weight [k] f32) of the gridded visibilities, channel by channel."""
+    table = np.ascontiguousarray(table, dtype=np.float32)
+    kern = GridKernel(table.shape[0], table.shape[1], int(support[0]), int(support[1]),
+                      table.ctypes.data_as(C.POINTER(C.c_float)))
+    C_ = len(freqs)
+    uvw_m = np.ascontiguousarray(uvw_m, dtype=np.float64)
+    vo = np.ascontiguousarray(vo, dtype=np.float32).reshape(-1, 2)
+    w = np.ascontiguousarray(weight, dtype=np.float32)
+    MN = int(M) * int(N)
+    ins, outs = (ChannelDesc * C_)(), (ChannelDesc * C_)()
+    bufs = []
+    for c in range(C_):
+        o, e = int(chan_off[c]), int(chan_off[c + 1])
+        ins[c] = ChannelDesc(float(np.float32(freqs[c])), e - o,
+                             uvw_m[o:e].ctypes.data_as(C.POINTER(C.c_double)),
+                             vo[o:e].ctypes.data_as(C.POINTER(C.c_float)),
+                             w[o:e].ctypes.data_as(C.POINTER(C.c_float)))
+        ou, ov, ow = np.zeros((MN, 3)), np.zeros((MN, 2), np.float32), np.zeros(MN, np.float32)
+        bufs.append((ou, ov, ow))
+        outs[c] = ChannelDesc(0.0, 0, ou.ctypes.data_as(C.POINTER(C.c_double)),
+                              ov.ctypes.data_as(C.POINTER(C.c_float)),
+                              ow.ctypes.data_as(C.POINTER(C.c_float)))
+    check(lib().gv_grid_visibilities(C.byref(kern), int(M), int(N), float(deltax_deg),
+                                     float(deltay_deg), C_, ins, outs, None))
+    counts = [int(outs[c].nvis) for c in range(C_)]
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return (off, np.concatenate([b[0][:k] for b, k in zip(bufs, counts)]),
+            np.concatenate([b[1][:k] for b, k in zip(bufs, counts)]),
+            np.concatenate([b[2][:k] for b, k in zip(bufs, counts)]))
+
+
+def grid(data, kind="PillBox2D", m=None, n=None, **params):
+    """The reference's gridding step for a synthetic data set (after its
+    weighting scheme): returns (gridded data, gcf) -- pass gcf to Problem."""
+    import dataclasses
+    table, sup, gcf = ckernel_build(kind, data.M, data.N, data.DELTAX, data.DELTAY, m, n,
+                                    **params)
+    off, uvw, vo, w = grid_visibilities(table, sup, data.M, data.N, data.DELTAX, data.DELTAY,
+                                        data.freqs, data.chan_off, data.uvw_m, data.vo,
+                                        data.weight)
+    return dataclasses.replace(data, chan_off=off, uvw_m=uvw, vo=vo, weight=w), gcf
+
+
+def _fp_tolerance(x1, x0):
+    """tolFunction (src/fixedpoint.cu:3-18): the largest relative change
+    |x1[i] - x0[i]| / |x0[i]| over the entries after the first (0 where x0[i]
+    is 0), in FP32."""
+    tol = [np.float32(0.0) if np.float32(abs(np.float32(x0[i]))) == 0.0 else
+           np.float32(abs(np.float32(x1[i]) - np.float32(x0[i]))) /
+           np.float32(abs(np.float32(x0[i]))) for i in range(1, len(x1))]
+    return float(max(tol)) if tol else 0.0
+
+
+def fixed_point_opt(guess, optf, tol, iterations):
+    """fixedPointOpt (src/fixedpoint.cu:32-57): iterates x1 = optf(x0) until
+    the relative change is at most `tol`, `iterations` are done or an entry
+    after the first reaches 1.  Kept as the reference runs it: the start point
+    is reused for the first two calls (x0 advances from the third on), and the
+    first tolerance is taken against a zero vector.  `optf` maps a list of
+    floats (e.g. penalization factors) to a list of floats; it typically
+    solves a problem with them."""
+    x0 = [float(v) for v in guess]
+    x1 = [0.0] * len(x0)
+    it = 0
+    c_tol = _fp_tolerance(x1, x0)
+    while it < iterations and c_tol > tol:
+        if it > 1:
+            x0 = x1
+        x1 = [float(np.float32(v)) for v in optf(list(x0))]
+        c_tol = _fp_tolerance(x1, x0)
+        if any(v >= 1.0 for v in x1[1:]):
+            break
+        it += 1
+    return x1

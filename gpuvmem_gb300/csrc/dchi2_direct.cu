@@ -33,6 +33,7 @@ struct DirectParams {
   int c_begin, c_end;
   int mode;  // 0 gradient (chain rule, 2 planes), 1 raw channel, 2 dirty image, 3 PSF,
              // 4 error-map sum: Re(w Vr e^{+2 pi i (x u + y v)}), no w-term
+  const float* gcf;  // gridding correction (modes 0, 1), or null
 };
 
 template <bool kDirty>
@@ -110,7 +111,10 @@ __global__ void __launch_bounds__(256) k_dchi2_direct(
     const float freq = chfreq[c];
     const float atten = attenuation(i, j, dp.xobs, dp.yobs, dp.DELTAX, dp.DELTAY, freq, dp.D,
                                     dp.pbf, dp.pbcut, dp.pb);
-    float d = (float)acc * (dp.fg_scale * atten);
+    // fg_scale * atten (* gcf: the GCF variant, src/functions.cu:3834-3836)
+    float sf = dp.fg_scale * atten;
+    if (dp.gcf) sf *= dp.gcf[q];
+    float d = (float)acc * sf;
     if (dp.normalize) d /= (float)chnvis[c];
     d = -d;
     if (dp.mode == 1) {
@@ -164,6 +168,7 @@ gv_status dchi2_direct(Problem& P, const float* d_img, int flag_opt, float* d_re
   dp.c_begin = only_channel >= 0 ? only_channel : 0;
   dp.c_end = only_channel >= 0 ? only_channel + 1 : (int)P.chans.size();
   dp.mode = mode;
+  dp.gcf = P.d_gcf;
   dim3 block(16, 16), grid((P.M + 15) / 16, (P.N + 15) / 16);
   if (mode >= 2) {
     k_dchi2_direct<true><<<grid, block, 0, P.stream>>>(

@@ -126,6 +126,7 @@ struct TcParams {
   const uint8_t* mask;
   const float* img;
   const uint32_t* cmax_bits;  // max |c| (float bits)
+  const float* gcf;           // [MN] gridding correction (modes 0, 1), or null
   float* partial;             // [nsplit][MN]
   uint32_t* err;
 };
@@ -160,7 +161,10 @@ __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int
   const float freq = p.chfreq[c];
   const float atten = attenuation(i, j, p.xobs, p.yobs, p.DELTAX, p.DELTAY, freq, p.D, p.pbf,
                                   p.pbcut, p.pb);
-  float f = -(p.fg_scale * atten) * inv_s;
+  // fg_scale * atten (* gcf: the GCF variant, src/functions.cu:3834-3836)
+  float sf = p.fg_scale * atten;
+  if (p.gcf) sf *= p.gcf[q];
+  float f = -sf * inv_s;
   if (p.normalize) f /= (float)p.chnvis[c];
   if (p.mode == 1) return f;
   const float nudiv = freq / p.nu_0;
@@ -850,6 +854,7 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
   p.partial = P.tc_partial;
   p.err = P.d_flags + kFlagErr;
   p.cmax_bits = P.d_flags + (mode == 2 ? kFlagDirtyMax : (mode == 3 ? kFlagPsfMax : kFlagCvrMax));
+  p.gcf = P.d_gcf;
   if (only_channel >= 0) {
     p.C = 1;
     p.kc_off = P.d_kc_one + 2 * only_channel;

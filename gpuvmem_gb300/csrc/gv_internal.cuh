@@ -64,6 +64,8 @@ struct Term {
   float prior_value;
   float eta;
   float epsilon;
+  float epsilon_b = 0.0f;
+  float* d_prior = nullptr;  // [MN] GEntropy / GL1Norm prior image (owned by the Problem)
 };
 
 // Packed per-visibility streams, sorted by grid cell within each channel.
@@ -100,6 +102,7 @@ struct Problem {
   float* d_wl = nullptr;
   int64_t* d_perm = nullptr;     // sorted position -> caller's index
   float* d_noise = nullptr;      // [MN]
+  float* d_gcf = nullptr;        // [MN] gridding correction of gridded data, or null
   uint8_t* d_mask = nullptr;     // [MN]
   float* d_rho = nullptr;        // [MN] z - 1 + r^2/2 per pixel
   float2* d_grid = nullptr;      // [C][MN] model grids

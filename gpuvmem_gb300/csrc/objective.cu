@@ -65,6 +65,7 @@ struct StageParams {
   float eta, minpix, threshold, fg_scale;
   int flag_opt;
   int write_clip;
+  const float* gcf;  // gridding correction, or null
 };
 
 // Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
@@ -106,7 +107,9 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
     // apply_beam2I, src/functions.cu:2424-2444
     const float a = attenuation(i, j, sp.xobs, sp.yobs, sp.DELTAX, sp.DELTAY, freq, sp.D,
                                 sp.pbf, sp.pbcut, sp.pb);
-    buf[bitrev(j, sp.log2n)] = make_float2(inu * a * sp.fg_scale, 0.0f);
+    float v = inu * a * sp.fg_scale;
+    if (sp.gcf) v *= sp.gcf[q];  // apply_GCF, src/functions.cu:2468
+    buf[bitrev(j, sp.log2n)] = make_float2(v, 0.0f);
   }
   __syncthreads();
   smem_fft(buf, sp.log2n, 1, tw);
@@ -242,11 +245,13 @@ struct PriorParams {
   int kind;
   int N;
   int64_t MN;
-  float lambda, G, eta, eps;
+  float lambda, G, eta, eps, eps_b;
+  const float* prior;  // GEntropy / GL1Norm prior image
 };
 
 // Value of one pixel, src/functions.cu:2882 (L1), 3036 (S), 3238 (TV),
-// 3353 (TSV), 3443 (L); the caller has checked the mask.
+// 3353 (TSV), 3443 (L), 3114 (SGVector), 2954 (GL1), 3141 (QP); the caller
+// has checked the mask.
 __device__ __forceinline__ float prior_pixel(const PriorParams& pp, const float* __restrict__ I,
                                              int i, int j) {
   const int N = pp.N;
@@ -277,12 +282,29 @@ __device__ __forceinline__ float prior_pixel(const PriorParams& pp, const float*
         return 0.5f * (Dx + Dy) * (Dx + Dy);
       }
       return c;
+    case GV_FI_GENTROPY: {
+      const float G = pp.prior[(int64_t)N * i + j];
+      return c * logf((c / G) + (pp.eta + 1.0f));
+    }
+    case GV_FI_GL1: {
+      const float g = pp.prior[(int64_t)N * i + j];
+      return sqrtf(c * c + pp.eps) / (sqrtf(g * g + pp.eps) + pp.eps_b);
+    }
+    case GV_FI_QUADRATIC:
+      if (i > 0 && i < N - 1 && j > 0 && j < N - 1) {
+        const float l = I[(int64_t)N * i + j - 1], r = I[(int64_t)N * i + j + 1];
+        const float d = I[(int64_t)N * (i + 1) + j], u = I[(int64_t)N * (i - 1) + j];
+        float qp = (c - l) * (c - l) + (c - r) * (c - r) + (c - u) * (c - u) + (c - d) * (c - d);
+        return qp / 2.0f;
+      }
+      return c;
   }
   return 0.0f;
 }
 
 // Gradient of one pixel before lambda, src/functions.cu:2917 (DL1), 3057
-// (DS), 3284 (DTV), 3395 (DTSV), 3488 (DL, with its d - r - u - l sign).
+// (DS), 3284 (DTV), 3395 (DTSV), 3488 (DL, with its d - r - u - l sign),
+// 3131 (DSG), 2993 (DGL1), 3190 (DQ, with its 4c - d + u + r + l).
 __device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
                                                   const float* __restrict__ I, int i, int j) {
   const int N = pp.N;
@@ -315,6 +337,17 @@ __device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
                P_(i + 2, j) + P_(i, j + 2) + P_(i - 2, j) + P_(i, j - 2);
       }
       return 0.0f;
+    case GV_FI_GENTROPY: {
+      const float G = pp.prior[(int64_t)N * i + j];
+      return logf((c / G) + (pp.eta + 1.0f)) + 1.0f / (1.0f + (((pp.eta + 1.0f) * G) / c));
+    }
+    case GV_FI_GL1: {
+      const float g = pp.prior[(int64_t)N * i + j];
+      return c / (sqrtf(c * c + pp.eps) * (sqrtf(g * g + pp.eps) + pp.eps_b));
+    }
+    case GV_FI_QUADRATIC:
+      if (inner) return 2.0f * (4.0f * c - P_(i + 1, j) + P_(i - 1, j) + P_(i, j + 1) + P_(i, j - 1));
+      return c;
   }
 #undef P_
   return 0.0f;
@@ -379,6 +412,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.fg_scale = P.fg_scale;
   sp.flag_opt = flag_opt;
   sp.write_clip = write_clip;
+  sp.gcf = P.d_gcf;
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
   const size_t sm1 = sizeof(float2) * (n + n / 2);
   if (sm1 > 48 * 1024)
@@ -427,6 +461,8 @@ static PriorParams prior_params(const Problem& P, const Term& t) {
   pp.G = t.prior_value;
   pp.eta = t.eta;
   pp.eps = t.epsilon;
+  pp.eps_b = t.epsilon_b;
+  pp.prior = t.d_prior;
   return pp;
 }
 

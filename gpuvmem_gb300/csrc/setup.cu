@@ -176,6 +176,8 @@ void free_problem(Problem& P) {
   cudaFree(P.d_wl);
   cudaFree(P.d_perm);
   cudaFree(P.d_noise);
+  cudaFree(P.d_gcf);
+  for (auto& t : P.terms) cudaFree(t.d_prior);
   cudaFree(P.d_mask);
   cudaFree(P.d_rho);
   cudaFree(P.d_grid);
@@ -250,7 +252,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
   // terms: ObjectiveFunction::addFi drops terms whose factor is 0
   for (int t = 0; t < d.nterms; t++) {
     const gv_fi_desc& f = d.terms[t];
-    if (f.kind < GV_FI_CHI2 || f.kind > GV_FI_LAPLACIAN) {
+    if (f.kind < GV_FI_CHI2 || f.kind > GV_FI_QUADRATIC) {
       set_error("unknown objective term kind");
       return GV_ERR_INVALID;
     }
@@ -263,8 +265,24 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
       set_error("Chi2 must be the first objective term (Chi2::addToDphi overwrites dphi)");
       return GV_ERR_INVALID;
     }
-    P.terms.push_back(Term{f.kind, f.lambda, f.image_index, f.image_to_add, f.prior_value,
-                           f.eta, f.epsilon});
+    Term tm{f.kind, f.lambda, f.image_index, f.image_to_add, f.prior_value, f.eta, f.epsilon};
+    tm.epsilon_b = f.epsilon_b;
+    if (f.kind == GV_FI_GENTROPY || f.kind == GV_FI_GL1) {
+      if (!f.prior_image) {
+        set_error("GEntropy and GL1Norm need a prior image");
+        return GV_ERR_INVALID;
+      }
+      // normalizePrior (src/gentropy.cu:123, src/gl1norm.cu:155): prior / factor
+      const int64_t MN = (int64_t)d.M * d.N;
+      std::vector<float> pr(f.prior_image, f.prior_image + MN);
+      const float nf = f.normalization_factor != 0.0f ? f.normalization_factor : 1.0f;
+      for (auto& v : pr) v /= nf;
+      GV_CUDA(cudaMalloc(&tm.d_prior, sizeof(float) * MN));
+      P.terms.push_back(tm);  // owned by P from here (freed by free_problem)
+      GV_CUDA(cudaMemcpy(tm.d_prior, pr.data(), sizeof(float) * MN, cudaMemcpyHostToDevice));
+      continue;
+    }
+    P.terms.push_back(tm);
   }
   int dev = 0;
   GV_CUDA(cudaGetDevice(&dev));
@@ -438,6 +456,12 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     P.max_wrho = maxw * rmax;
     cleanup();
 #undef GV_SETUP_CUDA
+  }
+
+  // ---- gridding correction function (Chi2::setCKernel with gridding) -------
+  if (d.gcf) {
+    GV_CUDA(cudaMalloc(&P.d_gcf, sizeof(float) * MN));
+    GV_CUDA(cudaMemcpyAsync(P.d_gcf, d.gcf, sizeof(float) * MN, cudaMemcpyHostToDevice, st));
   }
 
   // ---- noise image, mask, fg_scale, noise_cut ------------------------------

@@ -67,7 +67,10 @@ typedef enum gv_fi_kind {
   GV_FI_TSV = 2,       /* "TotalSquaredVariation" src/totalsquaredvariation.cu:44 */
   GV_FI_TV = 3,        /* "TotalVariation"        src/totalvariation.cu:60 */
   GV_FI_L1 = 4,        /* "L1-Norm"               src/l1norm.cu:57 */
-  GV_FI_LAPLACIAN = 5  /* "Laplacian"             src/laplacian.cu:43 */
+  GV_FI_LAPLACIAN = 5, /* "Laplacian"             src/laplacian.cu:43 */
+  GV_FI_GENTROPY = 6,  /* "GEntropy"  entropy against a prior image, src/gentropy.cu:131 */
+  GV_FI_GL1 = 7,       /* "GL1Norm"   L1 norm over a prior image,   src/gl1norm.cu:165 */
+  GV_FI_QUADRATIC = 8  /* "Quadratic" quadratic penalization, src/quadraticpenalization.cu:41 */
 } gv_fi_kind;
 
 typedef enum gv_beam { GV_BEAM_AIRYDISK = 0, GV_BEAM_GAUSSIAN = 1 } gv_beam;
@@ -80,7 +83,13 @@ typedef struct gv_fi_desc {
   int32_t image_to_add; /* plane its gradient is added to */
   float prior_value;    /* Entropy G (reference default set by main: 0.001) */
   float eta;            /* Entropy eta (reference default -1) */
-  float epsilon;        /* TV / L1 epsilon (reference default 1e-12) */
+  float epsilon;        /* TV / L1 epsilon; GL1Norm epsilon_a (reference default 1e-12) */
+  /* GEntropy / GL1Norm: the prior image (host, M*N floats), divided by
+   * normalization_factor at set-up as their normalizePrior does (0 counts as
+   * 1); GL1Norm's epsilon_b (reference default 1e-12) */
+  const float* prior_image;
+  float normalization_factor;
+  float epsilon_b;
 } gv_fi_desc;
 
 /* One spectral channel of one field with one correlation, as the
@@ -114,6 +123,11 @@ typedef struct gv_problem_desc {
   int32_t nterms;
   const gv_fi_desc* terms;
   int32_t dchi2_engine;     /* 0 auto, 1 direct SIMT, 2 tensor-core GEMM */
+  /* gridding correction function (host, M*N floats) of gridded data, or
+   * NULL: with it chi2() multiplies the beam-weighted image by it before the
+   * FFT (apply_GCF, src/functions.cu:2468) and DChi2 takes the GCF variant
+   * (src/functions.cu:3793-3888), as when Chi2::setCKernel was called */
+  const float* gcf;
 } gv_problem_desc;
 
 typedef struct gv_problem gv_problem;
@@ -281,6 +295,58 @@ gv_status gv_apply_weighting(int32_t scheme, float robust, int32_t M, int32_t N,
                              double deltax_deg, double deltay_deg, int32_t nchannels,
                              const gv_channel_desc* channels, float* const* weights_out,
                              void* stream);
+
+/* Convolution kernels of the gridding path (the CKernel family,
+ * include/classes/ckernel.cuh; src/pillBox2D.cu, src/gaussian2D.cu,
+ * src/sinc2D.cu, src/gaussianSinc2D.cu, src/pswf_12D.cu; ids as their
+ * registrations: "PillBox2D", "Gaussian2D", "Sinc2D", "GaussianSinc2D",
+ * "PSWF").  gv_ckernel_defaults fills what the reference's (m, n)
+ * constructor sets (PillBox2D's default constructor is 1 x 1). */
+typedef enum gv_ckernel_kind {
+  GV_CKERNEL_PILLBOX = 0,
+  GV_CKERNEL_GAUSSIAN = 1,
+  GV_CKERNEL_SINC = 2,
+  GV_CKERNEL_GAUSSIAN_SINC = 3,
+  GV_CKERNEL_PSWF = 4
+} gv_ckernel_kind;
+typedef struct gv_ckernel_desc {
+  int32_t kind;
+  int32_t m, n;  /* table rows and columns; supports are floor(m/2) in x and y */
+  float amp;     /* 1 */
+  float w;       /* width in cells: Gaussian, Sinc 1; GaussianSinc 2.52; PSWF 6 */
+  float alpha;   /* Gaussian exponent, 2 */
+  float w2;      /* GaussianSinc's sinc width, 1.55 */
+} gv_ckernel_desc;
+gv_status gv_ckernel_defaults(int32_t kind, int32_t m, int32_t n, gv_ckernel_desc* out);
+/* MFS::configure's kernel set-up (src/mfs.cu:510-516): the m x n table with
+ * cell sizes |deltau|, |deltav| (buildKernel) and the M x N gridding
+ * correction function with cell sizes |deltax|, |deltay| in radians
+ * (initializeGCF).  kernel: m*n floats; gcf: M*N floats or NULL.  has_gcf
+ * is 0 for Sinc2D and GaussianSinc2D, which define no GCF (the reference
+ * then reads an unset table); the GCF stays unused for them here. */
+gv_status gv_ckernel_build(const gv_ckernel_desc* k, int32_t M, int32_t N, double deltax_deg,
+                           double deltay_deg, float* kernel, int32_t* support_x,
+                           int32_t* support_y, float* gcf, int32_t* has_gcf);
+
+/* A convolution-kernel table as do_gridding reads it (getm, getn,
+ * getSupportX/Y, getKernelValue). */
+typedef struct gv_grid_kernel {
+  int32_t m, n, support_x, support_y;
+  const float* values;  /* host, m*n row-major */
+} gv_grid_kernel;
+/* do_gridding (src/functions.cu:1339-1653) on the GPU: each channel's
+ * visibilities and their Hermitian copies are convolved onto the M x N
+ * grid (weights, squared-kernel weights and weighted visibilities), each
+ * occupied cell's visibility is divided by its weight sum and gets the
+ * effective weight ws^2 / sum(w k^2), and the cells with a positive weight
+ * become the new visibilities, in row-major cell order, at the cell's
+ * (u, v) in metres with w = 0.  in[c]: host uvw (metres), Vo, weights;
+ * out[c]: host arrays of capacity M*N (uvw 3*M*N doubles, vo 2*M*N floats,
+ * weight M*N floats); out[c].nvis and freq_hz are written.  The result
+ * equals the reference's with one OpenMP thread bit for bit. */
+gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t M, int32_t N,
+                               double deltax_deg, double deltay_deg, int32_t nchannels,
+                               const gv_channel_desc* in, gv_channel_desc* out, void* stream);
 
 /* Autotuner (the reference takes its launch shapes from the -X/-Y/-V
  * flags, src/main.cu; here they are measured): times the candidates of the

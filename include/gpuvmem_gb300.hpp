@@ -79,7 +79,7 @@ class Fi {
   void calcGi(float* d_p, float* d_xi);
 
   gv_fi_desc desc() const {
-    gv_fi_desc d;
+    gv_fi_desc d{};
     d.kind = (int32_t)kind_;
     d.lambda = lambda_;
     d.image_index = image_index_;
@@ -87,8 +87,17 @@ class Fi {
     d.prior_value = prior_;
     d.eta = eta_;
     d.epsilon = epsilon_;
+    d.prior_image = prior_image_.empty() ? nullptr : prior_image_.data();
+    d.normalization_factor = normalization_factor_;
+    d.epsilon_b = epsilon_b_;
     return d;
   }
+
+ protected:
+  // GEntropy / GL1Norm: a host copy of the prior image (M*N floats), its
+  // normalisation factor and GL1Norm's epsilon_b
+  std::vector<float> prior_image_;
+  float normalization_factor_ = 1.0f, epsilon_b_ = 1e-12f;
 
  private:
   friend class ObjectiveFunction;
@@ -121,6 +130,41 @@ struct L1Norm : Fi {
 };
 struct Laplacian : Fi {
   Laplacian() : Fi(GV_FI_LAPLACIAN, "Laplacian") {}
+};
+// GEntropy(prior, normalization_factor, eta) (src/gentropy.cu:32): entropy
+// against a prior image (divided by the factor) instead of the constant G
+struct GEntropy : Fi {
+  GEntropy() : Fi(GV_FI_GENTROPY, "GEntropy") {}
+  GEntropy(std::vector<float> prior, float normalization_factor = 1.0f, float eta = -1.0f)
+      : Fi(GV_FI_GENTROPY, "GEntropy") {
+    setPriorImage(std::move(prior), normalization_factor);
+    setEta(eta);
+  }
+  void setPriorImage(std::vector<float> prior, float normalization_factor = 1.0f) {
+    prior_image_ = std::move(prior);
+    normalization_factor_ = normalization_factor;
+  }
+  float getNormalizationFactor() const { return normalization_factor_; }
+};
+// GL1Norm(prior, normalization_factor, epsilon_a, epsilon_b) (src/gl1norm.cu:42)
+struct GL1Norm : Fi {
+  GL1Norm() : Fi(GV_FI_GL1, "GL1Norm") {}
+  GL1Norm(std::vector<float> prior, float normalization_factor = 1.0f, float epsilon_a = 1e-12f,
+          float epsilon_b = 1e-12f)
+      : Fi(GV_FI_GL1, "GL1Norm") {
+    setPriorImage(std::move(prior), normalization_factor);
+    setEpsilon(epsilon_a);
+    epsilon_b_ = epsilon_b;
+  }
+  void setPriorImage(std::vector<float> prior, float normalization_factor = 1.0f) {
+    prior_image_ = std::move(prior);
+    normalization_factor_ = normalization_factor;
+  }
+  void setEpsilonB(float e) { epsilon_b_ = e; }
+};
+// QuadraticP, registered as "Quadratic" (src/quadraticpenalization.cu:41)
+struct QuadraticP : Fi {
+  QuadraticP() : Fi(GV_FI_QUADRATIC, "Quadratic") {}
 };
 
 // ------------------------------------------------------ ObjectiveFunction
@@ -263,6 +307,40 @@ inline void Fi::calcGi(float* d_p, float* d_xi) {
     status_ = gv_prior_gradient(of_->prob_, term_, d_p, d_xi);
 }
 
+// ---------------------------------------------------------- fixedPointOpt
+// fixedPointOpt (src/fixedpoint.cu:32-57) with its tolFunction (:3-18):
+// iterates x1 = optf(x0) until the largest relative change of the entries
+// after the first is at most tol, `iterations` are done, or an entry after
+// the first reaches 1.  As the reference runs it, x0 advances only from the
+// third call on and the first tolerance is taken against a zero vector.
+inline float fixedPointTolerance(const std::vector<float>& x1, const std::vector<float>& x0) {
+  float mx = 0.0f;
+  for (size_t i = 1; i < x1.size(); i++) {
+    const float a = x0[i] < 0.0f ? -x0[i] : x0[i];
+    const float d = x1[i] - x0[i];
+    const float t = a == 0.0f ? 0.0f : (d < 0.0f ? -d : d) / a;
+    if (i == 1 || t > mx) mx = t;
+  }
+  return mx;
+}
+template <class F>
+std::vector<float> fixedPointOpt(std::vector<float> guess, F optf, float tol, int iterations) {
+  std::vector<float> x0 = std::move(guess);
+  std::vector<float> x1(x0.size(), 0.0f);
+  int it = 0;
+  float c_tol = fixedPointTolerance(x1, x0);
+  while (it < iterations && c_tol > tol) {
+    if (it > 1) x0 = x1;
+    x1 = optf(x0);
+    c_tol = fixedPointTolerance(x1, x0);
+    bool big = false;
+    for (size_t i = 1; i < x1.size(); i++) big = big || x1[i] >= 1.0f;
+    if (big) break;
+    it++;
+  }
+  return x1;
+}
+
 // -------------------------------------------------------------- Optimizer
 class Optimizer {
  public:
@@ -383,6 +461,9 @@ inline void registerAll() {
   registerCreationFunction<Fi>("TotalVariation", [] { return (Fi*)new TotalVariation(); });
   registerCreationFunction<Fi>("L1-Norm", [] { return (Fi*)new L1Norm(); });
   registerCreationFunction<Fi>("Laplacian", [] { return (Fi*)new Laplacian(); });
+  registerCreationFunction<Fi>("GEntropy", [] { return (Fi*)new GEntropy(); });
+  registerCreationFunction<Fi>("GL1Norm", [] { return (Fi*)new GL1Norm(); });
+  registerCreationFunction<Fi>("Quadratic", [] { return (Fi*)new QuadraticP(); });
   registerCreationFunction<Optimizer>("CG-FRPRMN",
                                       [] { return (Optimizer*)new ConjugateGradient(); });
   registerCreationFunction<Optimizer>("CG-LBFGS", [] { return (Optimizer*)new LBFGS(); });

@@ -270,6 +270,8 @@ static void or_channel_grid(const or_problem* p, int c, const float* img,
                                      p->pb_factor, p->pb_cutoff,
                                      p->primary_beam);
       grid[2 * q] = inu * a * p->fg_scale;
+      /* apply_GCF, src/functions.cu:2468 (gridded data) */
+      if (p->gcf) grid[2 * q] *= (double)p->gcf[q];
       grid[2 * q + 1] = 0.0;
     }
   or_fft2d_inverse(N, grid);
@@ -402,6 +404,8 @@ void or_dchi2_channel(const or_problem* p, int c, const double* vr,
         s += w * (vr[2 * g] * cs + vr[2 * g + 1] * sn);
       }
       s *= (double)p->fg_scale * (double)a;
+      /* the GCF variant of DChi2, src/functions.cu:3793-3888 */
+      if (p->gcf) s *= (double)p->gcf[q];
       if (p->normalize) s /= (double)n;
       out[q] = -s;
     }
@@ -503,6 +507,26 @@ double or_prior_value(const or_problem* p, const or_term* t, const float* img) {
             v = c;
           }
           break;
+        case OR_FI_GENTROPY: { /* SGVector :3114 (calculateS with G = prior) */
+          const double G = t->prior_image[(int64_t)N * i + j];
+          v = c * log(c / G + (t->eta + 1.0));
+          break;
+        }
+        case OR_FI_GL1: { /* calculateGL1norm :2954 */
+          const double g = t->prior_image[(int64_t)N * i + j];
+          v = sqrt(c * c + t->epsilon) / (sqrt(g * g + t->epsilon) + t->epsilon_b);
+          break;
+        }
+        case OR_FI_QUADRATIC: /* calculateQP :3141 */
+          if (i > 0 && i < N - 1 && j > 0 && j < N - 1) {
+            const double l = PIX(i, j - 1), r = PIX(i, j + 1);
+            const double d = PIX(i + 1, j), u = PIX(i - 1, j);
+            v = ((c - l) * (c - l) + (c - r) * (c - r) + (c - u) * (c - u) +
+                 (c - d) * (c - d)) / 2.0;
+          } else {
+            v = c;
+          }
+          break;
         default:
           break;
       }
@@ -563,6 +587,22 @@ void or_prior_grad(const or_problem* p, const or_term* t, const float* img,
             } else {
               g = 0.0;
             }
+            break;
+          case OR_FI_GENTROPY: { /* DSG :3131 (calculateDS with G = prior) */
+            const double G = t->prior_image[q];
+            g = log(c / G + (t->eta + 1.0)) + 1.0 / (1.0 + ((t->eta + 1.0) * G) / c);
+            break;
+          }
+          case OR_FI_GL1: { /* calculateDGNormL1 :2993 */
+            const double pr = t->prior_image[q];
+            g = c / (sqrt(c * c + t->epsilon) *
+                     (sqrt(pr * pr + t->epsilon) + t->epsilon_b));
+            break;
+          }
+          case OR_FI_QUADRATIC: /* calculateDQ :3190 (its 4c - d + u + r + l kept) */
+            g = inner ? 2.0 * (4.0 * c - PIX(i + 1, j) + PIX(i - 1, j) + PIX(i, j + 1) +
+                               PIX(i, j - 1))
+                      : c;
             break;
           default:
             break;

@@ -54,7 +54,10 @@ enum {
   OR_FI_TSV = 2,
   OR_FI_TV = 3,
   OR_FI_L1 = 4,
-  OR_FI_LAPLACIAN = 5
+  OR_FI_LAPLACIAN = 5,
+  OR_FI_GENTROPY = 6,  /* entropy against a prior image, src/gentropy.cu */
+  OR_FI_GL1 = 7,       /* L1 norm weighted by a prior image, src/gl1norm.cu */
+  OR_FI_QUADRATIC = 8  /* quadratic penalization, src/quadraticpenalization.cu */
 };
 
 typedef struct or_term {
@@ -64,7 +67,9 @@ typedef struct or_term {
   int image_to_add;  /* plane its gradient is added to */
   float prior_value; /* entropy G */
   float eta;         /* entropy eta */
-  float epsilon;     /* TV / L1 epsilon */
+  float epsilon;     /* TV / L1 epsilon; GL1Norm epsilon_a */
+  const float* prior_image; /* [M*N] GEntropy / GL1Norm prior (already normalised) */
+  float epsilon_b;   /* GL1Norm epsilon_b */
 } or_term;
 
 /* One imaging problem: one field, nchan channels, one correlation each. */
@@ -88,6 +93,7 @@ typedef struct or_problem {
   const float* noise;     /* [M*N] noise image */
   int nterms;
   const or_term* terms;   /* Chi2 first, as the reference requires */
+  const float* gcf;       /* [M*N] gridding correction of gridded data, or NULL */
 } or_problem;
 
 /* ---- set-up ---------------------------------------------------------- */

@@ -16,13 +16,15 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 OR_AIRYDISK, OR_GAUSSIAN = 0, 1
-FI_CHI2, FI_ENTROPY, FI_TSV, FI_TV, FI_L1, FI_LAPLACIAN = range(6)
+FI_CHI2, FI_ENTROPY, FI_TSV, FI_TV, FI_L1, FI_LAPLACIAN, FI_GENTROPY, FI_GL1, FI_QUADRATIC = \
+    range(9)
 
 
 class OrTerm(C.Structure):
     _fields_ = [("kind", C.c_int), ("lam", C.c_float), ("image_index", C.c_int),
                 ("image_to_add", C.c_int), ("prior_value", C.c_float),
-                ("eta", C.c_float), ("epsilon", C.c_float)]
+                ("eta", C.c_float), ("epsilon", C.c_float),
+                ("prior_image", C.POINTER(C.c_float)), ("epsilon_b", C.c_float)]
 
 
 class OrProblem(C.Structure):
@@ -36,7 +38,8 @@ class OrProblem(C.Structure):
                 ("freq", C.POINTER(C.c_float)), ("chan_off", C.POINTER(C.c_int64)),
                 ("uvw", C.POINTER(C.c_double)), ("vo", C.POINTER(C.c_float)),
                 ("weight", C.POINTER(C.c_float)), ("noise", C.POINTER(C.c_float)),
-                ("nterms", C.c_int), ("terms", C.POINTER(OrTerm))]
+                ("nterms", C.c_int), ("terms", C.POINTER(OrTerm)),
+                ("gcf", C.POINTER(C.c_float))]
 
 
 class OrState(C.Structure):
@@ -115,7 +118,7 @@ class Oracle:
     reference's MFS::setDevice and chi2()/dchi2() order."""
 
     def __init__(self, data, terms, eta=-1.0, initial_value=0.001, noise_cut=10.0,
-                 threshold=0.0, normalize=False, vis_noise=-1.0):
+                 threshold=0.0, normalize=False, vis_noise=-1.0, gcf=None):
         L = lib()
         self.data = data
         self.M, self.N = data.M, data.N
@@ -153,7 +156,15 @@ class Oracle:
         self.terms_list = list(terms)
         self.terms = (OrTerm * max(1, len(terms)))()
         for i, t in enumerate(terms):
-            self.terms[i] = OrTerm(*t)
+            self.terms[i] = OrTerm(*t[:7])
+            if len(t) > 7:
+                # GEntropy / GL1Norm: the prior image divided by its factor
+                # in FP32, as normalizePrior does
+                pr = (np.asarray(t[7], np.float32).reshape(-1) /
+                      np.float32(t[8] if t[8] else 1.0)).astype(np.float32)
+                self._priors = getattr(self, "_priors", []) + [pr]
+                self.terms[i].prior_image = _p(pr, C.c_float)
+                self.terms[i].epsilon_b = float(t[9])
         self.prob = OrProblem(
             self.M, self.N, data.DELTAX, data.DELTAY, data.xobs, data.yobs, data.nu_0,
             data.antenna_diameter, data.pb_factor, data.pb_cutoff, data.primary_beam,
@@ -161,6 +172,10 @@ class Oracle:
             nc, _p(self.freqs, C.c_float), _p(self.chan_off, C.c_int64),
             _p(self.uvw, C.c_double), _p(self.vo, C.c_float), _p(self.weight, C.c_float),
             _p(self.noise, C.c_float), len(terms), self.terms)
+        # gridding correction function of gridded data (apply_GCF / GCF DChi2)
+        self.gcf = None if gcf is None else np.ascontiguousarray(gcf, np.float32).reshape(-1)
+        if self.gcf is not None:
+            self.prob.gcf = _p(self.gcf, C.c_float)
         self.vr = np.zeros(2 * self.chan_off[-1], dtype=np.float64)
         self.state = OrState(C.pointer(self.prob), 0, 0, _p(self.vr, C.c_double),
                              (C.c_double * 8)(), 0, 0)

@@ -25,11 +25,12 @@ static int failures = 0;
 static int cpu_tests() {
   using namespace gvgb;
   registerAll();
-  const char* fis[] = {"Chi2", "Entropy", "TotalSquaredVariation", "TotalVariation", "L1-Norm",
-                       "Laplacian"};
-  const gv_fi_kind kinds[] = {GV_FI_CHI2, GV_FI_ENTROPY, GV_FI_TSV, GV_FI_TV, GV_FI_L1,
-                              GV_FI_LAPLACIAN};
-  for (int k = 0; k < 6; k++) {
+  const char* fis[] = {"Chi2",      "Entropy",  "TotalSquaredVariation", "TotalVariation",
+                       "L1-Norm",   "Laplacian", "GEntropy", "GL1Norm", "Quadratic"};
+  const gv_fi_kind kinds[] = {GV_FI_CHI2,      GV_FI_ENTROPY,  GV_FI_TSV, GV_FI_TV,
+                              GV_FI_L1,        GV_FI_LAPLACIAN, GV_FI_GENTROPY, GV_FI_GL1,
+                              GV_FI_QUADRATIC};
+  for (int k = 0; k < 9; k++) {
     std::unique_ptr<Fi> f(createObject<Fi>(fis[k]));
     CHECK(f != nullptr);
     if (f) {
@@ -41,6 +42,16 @@ static int cpu_tests() {
   std::unique_ptr<Optimizer> lb(createObject<Optimizer>("CG-LBFGS"));
   CHECK(cg && dynamic_cast<ConjugateGradient*>(cg.get()));
   CHECK(lb && dynamic_cast<LBFGS*>(lb.get()));
+  // fixedPointOpt: 0.3 -> 0.6 twice (x0 advances from the third call), then 1.2 stops it
+  int ncalls = 0;
+  std::vector<float> fp = fixedPointOpt(
+      std::vector<float>{0.1f, 0.3f},
+      [&](const std::vector<float>& x) {
+        ncalls++;
+        return std::vector<float>{x[0], 2.0f * x[1]};
+      },
+      1e-9f, 10);
+  CHECK(ncalls == 3 && fp.size() == 2 && fp[1] > 1.19f && fp[1] < 1.21f);
   CHECK(createObject<Fi>("NoSuchPrior") == nullptr);  // the reference exits here
   CHECK(createObject<Optimizer>("CG-NONE") == nullptr);
   CHECK(!registerCreationFunction<Fi>("Chi2", [] { return (Fi*)new Chi2(); }));

@@ -155,6 +155,57 @@ def test_prior_value_and_gradient(pair64, t):
     assert np.abs(got_g[add] - ref_g).max() <= 2e-5 * scale
 
 
+def _extra_priors(n):
+    """GEntropy and GL1Norm over a seeded prior image (factor 2 and 1), and
+    Quadratic; the prior stays below the image so every term is positive."""
+    rng = np.random.default_rng(77)
+    prior = rng.uniform(1e-4, 9e-4, (n, n)).astype(np.float32)
+    return [(O.FI_CHI2, 1.0, 0, 0, 0.0, 0.0, 0.0),
+            (O.FI_GENTROPY, 0.01, 0, 0, 0.0, -1.0, 0.0, prior, 2.0, 0.0),
+            (O.FI_GL1, 1e-3, 0, 0, 0.0, 0.0, 1e-12, prior, 1.0, 1e-12),
+            (O.FI_QUADRATIC, 1e-5, 0, 0, 0.0, 0.0, 0.0)]
+
+
+@pytest.fixture(scope="module")
+def pair64_extra():
+    return make_pair(synth.small_config(n=64, nchan=2, seed=3), _extra_priors(64))
+
+
+@pytest.mark.parametrize("t", range(1, 4))
+def test_extra_prior_value_and_gradient(pair64_extra, t):
+    """GEntropy (src/gentropy.cu), GL1Norm (src/gl1norm.cu) and Quadratic
+    (src/quadraticpenalization.cu) against the oracle."""
+    torch = _torch()
+    data, orc, prob = pair64_extra
+    img = rand_image(orc, 41 + t)
+    _, img = orc.chi2(img.copy())
+    d = torch.from_numpy(img.copy()).cuda()
+    ref_v = orc.prior_value(t, img)
+    got_v = prob.prior_value(t, d)
+    assert ref_v > 0
+    assert abs(got_v - ref_v) <= 1e-5 * ref_v, (got_v, ref_v)
+    ref_g = orc.prior_grad(t, img)
+    got_g = prob.prior_gradient(t, d).cpu().numpy()
+    scale = np.abs(ref_g).max()
+    assert scale > 0
+    assert np.abs(got_g[0] - ref_g).max() <= 2e-5 * scale
+
+
+def test_extra_priors_objective(pair64_extra):
+    """The whole objective with the three extra priors active (iteration 1)."""
+    torch = _torch()
+    data, orc, prob = pair64_extra
+    img = rand_image(orc, 51)
+    d = torch.from_numpy(img.copy()).cuda()
+    orc.state.iteration = 1
+    f_ref, _ = orc.calc_function(img.copy())
+    prob.set_iteration(1)
+    f_got, _ = prob.objective(d)
+    prob.set_iteration(0)
+    orc.state.iteration = 0
+    assert abs(f_got - f_ref) <= CHI2_RTOL * abs(f_ref), (f_got, f_ref)
+
+
 def test_objective_and_gradient_iteration_gating(pair64):
     torch = _torch()
     data, orc, prob = pair64
