@@ -8,10 +8,11 @@
 // in FP32 under OpenMP atomics and a critical section, so its sums depend on
 // the thread schedule; with one thread each cell is a sequential FP32 sum in
 // visibility order (the original visibilities, then their Hermitian copies).
-// Here the (cell, visibility) pairs of a slab of visibilities are radix
-// sorted as 64-bit keys (cell in the high bits, visibility in the low bits),
-// and one thread per occupied cell walks its run in visibility order,
-// continuing the cell's running sums from the previous slab.  That
+// Here the (cell, slot) pairs of a slab of visibilities, slot = visibility
+// x taps + tap, are radix sorted by cell with a stable (LSD) sort, so equal
+// cells keep visibility order; one warp per occupied cell walks its run, the
+// lanes forming 32 entries' products in parallel and one lane adding them in
+// order, continuing the cell's running sums from the previous slab.  That
 // reproduces the one-thread result bit for bit, with every product rounded
 // as the reference's host code rounds it (no contraction into FMAs).
 //
@@ -147,7 +148,7 @@ float gcf_value(const gv_ckernel_desc& k, int i, int j, int sup, float w, float 
 }
 
 // ---------------------------------------------------------------- device
-constexpr int64_t kMaxKeys = int64_t(1) << 27;  // (cell, visibility) keys per sorted slab
+constexpr int64_t kMaxKeys = int64_t(1) << 27;  // (cell, slot) pairs per sorted slab
 
 int bits_for(uint64_t v) {  // bits to hold 0..v
   int b = 1;
@@ -161,11 +162,11 @@ struct GridGeom {
   float lambda;
 };
 
-// cell of visibility z (z >= n: the Hermitian copy of z - n) and its keys,
-// one per kernel tap in the reference's loop order (src/functions.cu:1424-1474)
-__global__ void k_grid_keys(GridGeom g, int64_t n, int64_t z0, int64_t nz,
-                            const double* __restrict__ uvw, int zbits, uint64_t sentinel,
-                            int2* __restrict__ base, uint64_t* __restrict__ keys) {
+// cell of visibility z (z >= n: the Hermitian copy of z - n), as the
+// reference computes it (src/functions.cu:1424-1462): float wavelength, FP64
+// u / du + N/2 + 0.5 truncated
+__global__ void k_grid_cells(GridGeom g, int64_t n, int64_t z0, int64_t nz,
+                             const double* __restrict__ uvw, int2* __restrict__ base) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nz) return;
   const int64_t z = z0 + t;
@@ -178,58 +179,97 @@ __global__ void k_grid_keys(GridGeom g, int64_t n, int64_t z0, int64_t nz,
   }
   const double ul = __ddiv_rn(u, (double)g.lambda), vl = __ddiv_rn(v, (double)g.lambda);
   const double gx = __ddiv_rn(ul, g.deltau), gy = __ddiv_rn(vl, g.deltav);
-  const int j = (int)__dadd_rn(__dadd_rn(gx, g.cj), 0.5);
-  const int k = (int)__dadd_rn(__dadd_rn(gy, g.ck), 0.5);
-  base[t] = make_int2(j, k);
-  const int tw = 2 * g.sx + 1;
-  const int64_t T = (int64_t)(2 * g.sy + 1) * tw;
-  uint64_t* kp = keys + t * T;
-  for (int mm = -g.sy; mm <= g.sy; mm++) {
-    for (int nn = -g.sx; nn <= g.sx; nn++) {
-      const int sk = k + mm, sj = j + nn, ki = mm + g.sy, kj = nn + g.sx;
-      const bool ok = sk >= 0 && sk < g.M && sj >= 0 && sj < g.N && ki < g.km && kj < g.kn;
-      kp[ki * tw + kj] =
-          ok ? ((uint64_t)((int64_t)g.N * sk + sj) << zbits) | (uint64_t)t : sentinel;
-    }
-  }
+  base[t] = make_int2((int)__dadd_rn(__dadd_rn(gx, g.cj), 0.5),
+                      (int)__dadd_rn(__dadd_rn(gy, g.ck), 0.5));
 }
 
-// one thread per run of a cell in the sorted keys: the cell's sums continue
-// in visibility order (src/functions.cu:1476-1506)
-__global__ void k_grid_runs(GridGeom g, int64_t n, int64_t z0, int64_t nk,
-                            const uint64_t* __restrict__ skeys, int zbits,
-                            const int2* __restrict__ base, const float* __restrict__ w,
-                            const float2* __restrict__ vo, const float* __restrict__ ktab,
-                            float* __restrict__ gw, float* __restrict__ gaux,
-                            float2* __restrict__ gvo) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nk) return;
-  const uint64_t cell = skeys[i] >> zbits;  // the sentinel's cell field is >= M*N
-  if (cell >= (uint64_t)g.M * (uint64_t)g.N || (i > 0 && (skeys[i - 1] >> zbits) == cell)) return;
-  const uint64_t zmask = (1ull << zbits) - 1;
-  const int row = (int)(cell / (uint64_t)g.N), col = (int)(cell % (uint64_t)g.N);
-  float sw = gw[cell], sa = gaux[cell];
-  float2 sv = gvo[cell];
-  for (int64_t q = i; q < nk; q++) {
-    const uint64_t key = skeys[q];
-    if ((key >> zbits) != cell) break;
-    const int64_t t = (int64_t)(key & zmask);
-    const int2 b = base[t];
-    const float c = ktab[(row - b.y + g.sy) * g.kn + (col - b.x + g.sx)];
-    const int64_t z = z0 + t;
-    const bool herm = z >= n;
-    const int64_t vi = herm ? z - n : z;
-    const float wv = w[vi];
-    float2 V = vo[vi];
-    if (herm) V.y *= -1.0f;
-    sw = __fadd_rn(sw, __fmul_rn(wv, c));
-    sa = __fadd_rn(sa, __fmul_rn(wv, __fmul_rn(c, c)));
-    sv.x = __fadd_rn(sv.x, __fmul_rn(__fmul_rn(wv, V.x), c));
-    sv.y = __fadd_rn(sv.y, __fmul_rn(__fmul_rn(wv, V.y), c));
+// one (cell, slot) pair per slot = t * taps + tap, taps in the reference's
+// loop order (src/functions.cu:1466-1474); taps outside the grid or the
+// table get the all-ones cell
+__global__ void k_grid_keys(GridGeom g, int64_t nk, const int2* __restrict__ base,
+                            uint32_t* __restrict__ keys, uint32_t* __restrict__ slots) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= nk) return;
+  const int tw = 2 * g.sx + 1;
+  const int T = (2 * g.sy + 1) * tw;
+  const int64_t t = s / T;
+  const int tap = (int)(s - t * T);
+  const int ki = tap / tw, kj = tap - ki * tw;
+  const int2 b = base[t];
+  const int sk = b.y + ki - g.sy, sj = b.x + kj - g.sx;
+  const bool ok = sk >= 0 && sk < g.M && sj >= 0 && sj < g.N && ki < g.km && kj < g.kn;
+  keys[s] = ok ? (uint32_t)(g.N * sk + sj) : 0xFFFFFFFFu;
+  slots[s] = (uint32_t)s;
+}
+
+// one warp per run of a cell in the pairs sorted (stably) by cell
+// (src/functions.cu:1476-1506): the lanes gather 32 entries at a time and
+// form their rounded products (w k, w k^2, w Vo k) in parallel; lane 0 adds
+// them to the cell's running sums in visibility order, continuing from the
+// previous slab, so every sum is the reference's sequential FP32 sum
+constexpr int kRunWarps = 8;  // warps per block of k_grid_runs
+__global__ void __launch_bounds__(kRunWarps * 32) k_grid_runs(
+    GridGeom g, int64_t n, int64_t z0, const uint32_t* __restrict__ cells,
+    const uint32_t* __restrict__ starts, const uint32_t* __restrict__ counts,
+    const int* __restrict__ nruns, const uint32_t* __restrict__ sslots,
+    const float* __restrict__ w, const float2* __restrict__ vo, const float* __restrict__ ktab,
+    float* __restrict__ gw, float* __restrict__ gaux, float2* __restrict__ gvo) {
+  __shared__ float4 prod[kRunWarps][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int tw = 2 * g.sx + 1;
+  const int T = (2 * g.sy + 1) * tw;
+  const int64_t MN = (int64_t)g.M * g.N;
+  const int nr = *nruns;
+  for (int r = blockIdx.x * kRunWarps + wib; r < nr; r += gridDim.x * kRunWarps) {
+    const uint32_t cell = cells[r];
+    if ((int64_t)cell >= MN) continue;  // the run of unused taps
+    const uint32_t a = starts[r], e = a + counts[r];
+    float sw = 0.0f, sa = 0.0f, sx = 0.0f, sy = 0.0f;
+    if (lane == 0) {
+      sw = gw[cell];
+      sa = gaux[cell];
+      const float2 v = gvo[cell];
+      sx = v.x;
+      sy = v.y;
+    }
+    for (uint32_t b0 = a; b0 < e; b0 += 32) {
+      const uint32_t q = b0 + (uint32_t)lane;
+      float4 pr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (q < e) {
+        const uint32_t s = sslots[q];
+        const int64_t t = s / (uint32_t)T;
+        const int tap = (int)(s - (uint32_t)t * (uint32_t)T);
+        const int ki = tap / tw, kj = tap - ki * tw;
+        const float c = ktab[ki * g.kn + kj];
+        const int64_t z = z0 + t;
+        const bool herm = z >= n;
+        const int64_t vi = herm ? z - n : z;
+        const float wv = w[vi];
+        float2 V = vo[vi];
+        if (herm) V.y *= -1.0f;
+        pr = make_float4(__fmul_rn(wv, c), __fmul_rn(wv, __fmul_rn(c, c)),
+                         __fmul_rn(__fmul_rn(wv, V.x), c), __fmul_rn(__fmul_rn(wv, V.y), c));
+      }
+      prod[wib][lane] = pr;
+      __syncwarp();
+      if (lane == 0) {
+        const int m = (int)min((uint32_t)32, e - b0);
+        for (int l = 0; l < m; l++) {
+          const float4 p = prod[wib][l];
+          sw = __fadd_rn(sw, p.x);
+          sa = __fadd_rn(sa, p.y);
+          sx = __fadd_rn(sx, p.z);
+          sy = __fadd_rn(sy, p.w);
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      gw[cell] = sw;
+      gaux[cell] = sa;
+      gvo[cell] = make_float2(sx, sy);
+    }
   }
-  gw[cell] = sw;
-  gaux[cell] = sa;
-  gvo[cell] = sv;
 }
 
 // normalisation and effective weight (src/functions.cu:1514-1567)
@@ -274,7 +314,9 @@ struct GridBuffers {
   float* w = nullptr;
   float2* vo = nullptr;
   int2* base = nullptr;
-  uint64_t *keys = nullptr, *skeys = nullptr;
+  uint32_t *keys = nullptr, *skeys = nullptr, *slots = nullptr, *sslots = nullptr;
+  uint32_t *rcell = nullptr, *rcount = nullptr, *rstart = nullptr;
+  int* nruns = nullptr;
   float *gw = nullptr, *gaux = nullptr, *ktab = nullptr;
   float2* gvo = nullptr;
   int *flag = nullptr, *pos = nullptr;
@@ -289,6 +331,12 @@ struct GridBuffers {
     cudaFree(base);
     cudaFree(keys);
     cudaFree(skeys);
+    cudaFree(slots);
+    cudaFree(sslots);
+    cudaFree(rcell);
+    cudaFree(rcount);
+    cudaFree(rstart);
+    cudaFree(nruns);
     cudaFree(gw);
     cudaFree(gaux);
     cudaFree(ktab);
@@ -394,15 +442,23 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
   for (int c = 0; c < nchannels; c++) vmax = std::max<int64_t>(vmax, in[c].nvis);
   const int64_t zslab = std::max<int64_t>(1, std::min<int64_t>(2 * vmax, kMaxKeys / T));
   const int64_t kcap = zslab * T;
-  const int cellbits = bits_for((uint64_t)MN);  // the all-ones cell field is no cell
+  const int cellbits = bits_for((uint64_t)MN);  // the all-ones cell is no cell
   cudaStream_t st = (cudaStream_t)stream;
   GridBuffers b;
   GV_CUDA(cudaMalloc(&b.uvw, sizeof(double) * 3 * vmax));
   GV_CUDA(cudaMalloc(&b.w, sizeof(float) * vmax));
   GV_CUDA(cudaMalloc(&b.vo, sizeof(float2) * vmax));
   GV_CUDA(cudaMalloc(&b.base, sizeof(int2) * zslab));
-  GV_CUDA(cudaMalloc(&b.keys, sizeof(uint64_t) * kcap));
-  GV_CUDA(cudaMalloc(&b.skeys, sizeof(uint64_t) * kcap));
+  GV_CUDA(cudaMalloc(&b.keys, sizeof(uint32_t) * kcap));
+  GV_CUDA(cudaMalloc(&b.skeys, sizeof(uint32_t) * kcap));
+  GV_CUDA(cudaMalloc(&b.slots, sizeof(uint32_t) * kcap));
+  GV_CUDA(cudaMalloc(&b.sslots, sizeof(uint32_t) * kcap));
+  // runs of equal cells in a slab: at most one per cell plus the unused taps'
+  const int64_t rcap = std::min<int64_t>(kcap, MN + 1);
+  GV_CUDA(cudaMalloc(&b.rcell, sizeof(uint32_t) * rcap));
+  GV_CUDA(cudaMalloc(&b.rcount, sizeof(uint32_t) * rcap));
+  GV_CUDA(cudaMalloc(&b.rstart, sizeof(uint32_t) * rcap));
+  GV_CUDA(cudaMalloc(&b.nruns, sizeof(int)));
   GV_CUDA(cudaMalloc(&b.gw, sizeof(float) * MN));
   GV_CUDA(cudaMalloc(&b.gaux, sizeof(float) * MN));
   GV_CUDA(cudaMalloc(&b.gvo, sizeof(float2) * MN));
@@ -414,11 +470,15 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
   GV_CUDA(cudaMalloc(&b.ktab, sizeof(float) * kernel->m * kernel->n));
   GV_CUDA(cudaMemcpyAsync(b.ktab, kernel->values, sizeof(float) * kernel->m * kernel->n,
                           cudaMemcpyHostToDevice, st));
-  size_t sort_bytes = 0, scan_bytes = 0;
-  GV_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, b.keys, b.skeys, (int)kcap, 0, 64,
-                                         st));
+  size_t sort_bytes = 0, scan_bytes = 0, rle_bytes = 0, rscan_bytes = 0;
+  GV_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, b.keys, b.skeys, b.slots, b.sslots,
+                                          (int)kcap, 0, cellbits, st));
   GV_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, b.flag, b.pos, (int)MN, st));
-  const size_t tmp_bytes = std::max(sort_bytes, scan_bytes);
+  GV_CUDA(cub::DeviceRunLengthEncode::Encode(nullptr, rle_bytes, b.skeys, b.rcell, b.rcount,
+                                             b.nruns, (int)kcap, st));
+  GV_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, rscan_bytes, b.rcount, b.rstart, (int)rcap, st));
+  const size_t tmp_bytes =
+      std::max(std::max(sort_bytes, scan_bytes), std::max(rle_bytes, rscan_bytes));
   GV_CUDA(cudaMalloc(&b.tmp, tmp_bytes));
   for (int c = 0; c < nchannels; c++) {
     const int64_t n = in[c].nvis;
@@ -435,17 +495,27 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
     for (int64_t z0 = 0; z0 < 2 * n; z0 += zslab) {
       const int64_t nz = std::min<int64_t>(zslab, 2 * n - z0);
       const int64_t nk = nz * T;
-      const int zbits = bits_for((uint64_t)(nz - 1));
-      const int end_bit = std::min(64, zbits + cellbits);
-      const uint64_t sentinel = end_bit >= 64 ? ~0ull : ((1ull << end_bit) - 1);
-      k_grid_keys<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(g, n, z0, nz, b.uvw, zbits,
-                                                                sentinel, b.base, b.keys);
+      k_grid_cells<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(g, n, z0, nz, b.uvw, b.base);
+      GV_LAUNCH("k_grid_cells");
+      k_grid_keys<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(g, nk, b.base, b.keys, b.slots);
       GV_LAUNCH("k_grid_keys");
       size_t tb = tmp_bytes;
-      GV_CUDA(cub::DeviceRadixSort::SortKeys(b.tmp, tb, b.keys, b.skeys, (int)nk, 0, end_bit, st));
-      add_launches(1);
-      k_grid_runs<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(
-          g, n, z0, nk, b.skeys, zbits, b.base, b.w, b.vo, b.ktab, b.gw, b.gaux, b.gvo);
+      GV_CUDA(cub::DeviceRadixSort::SortPairs(b.tmp, tb, b.keys, b.skeys, b.slots, b.sslots,
+                                              (int)nk, 0, cellbits, st));
+      tb = tmp_bytes;
+      GV_CUDA(cub::DeviceRunLengthEncode::Encode(b.tmp, tb, b.skeys, b.rcell, b.rcount, b.nruns,
+                                                 (int)nk, st));
+      // run starts: exclusive sum of the run lengths (over the capacity; the
+      // entries past the run count are not read)
+      const int64_t nr_cap = std::min<int64_t>(nk, rcap);
+      tb = tmp_bytes;
+      GV_CUDA(cub::DeviceScan::ExclusiveSum(b.tmp, tb, b.rcount, b.rstart, (int)nr_cap, st));
+      add_launches(3);
+      const unsigned rb = (unsigned)std::min<int64_t>((nr_cap + kRunWarps - 1) / kRunWarps,
+                                                      (int64_t)65535 * 16);
+      k_grid_runs<<<rb, kRunWarps * 32, 0, st>>>(g, n, z0, b.rcell, b.rstart, b.rcount, b.nruns,
+                                                 b.sslots, b.w, b.vo, b.ktab, b.gw, b.gaux,
+                                                 b.gvo);
       GV_LAUNCH("k_grid_runs");
     }
     const unsigned gb = (unsigned)((MN + 255) / 256);
