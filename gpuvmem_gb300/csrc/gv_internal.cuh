@@ -41,6 +41,8 @@ enum FlagSlot {
   kFlagDirtyMax = 1,  // max |w Vo| component (float bits)
   kFlagErr = 2,       // non-zero: a kernel gave up on a bounded wait
   kFlagPsfMax = 3,    // max weight of a kept visibility (float bits)
+  kFlagDegridDone = 4,  // blocks of k_degrid done (the last one finishes chi2)
+  kFlagPriorDone = 5,   // blocks of k_prior_value done (the last one sums)
   kNumFlags = 8
 };
 

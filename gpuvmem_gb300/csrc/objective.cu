@@ -168,12 +168,52 @@ __device__ double block_sum(double v) {
   return v;
 }
 
-// Pass 3: vis_mod + residual + chi2Vector + partial reduction.
+// True in every thread of the block that finishes last of `nblocks` (after
+// each block stored its partial); that block resets the counter for the next
+// launch.  The last block then sums the partials in a fixed order, so the
+// result does not depend on which block finished last.
+__device__ bool last_block_done(uint32_t* counter, uint32_t nblocks) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t prev = atomicAdd(counter, 1u);
+    last = prev == nblocks - 1 ? 1 : 0;
+    if (last) *counter = 0u;
+  }
+  __syncthreads();
+  return last != 0;
+}
+
+// Sum of channel partials in a fixed order; writes 0.5 * sum to out
+// (chi2(), src/functions.cu:4408-4451: per channel /V when normalize).
+__device__ void finish_chi2(int C, int nb, const double* part, int part_stride,
+                            const int64_t* __restrict__ nvis, int normalize, double* out) {
+  __shared__ double tot;
+  if (threadIdx.x == 0) tot = 0.0;
+  __syncthreads();
+  for (int c = 0; c < C; c++) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += __ldcg(part + (int64_t)c * part_stride + b);
+    v = block_sum(v);
+    if (threadIdx.x == 0) {
+      if (normalize && nvis[c] > 0) v /= (double)nvis[c];
+      tot += v;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = 0.5 * tot;
+}
+
+// Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
+// block to finish adds the partials into the chi2 scalar.
 __global__ void __launch_bounds__(256) k_degrid(
     int N, int64_t MN, const ChanRange* __restrict__ ranges,
     const float4* __restrict__ deg, const float2* __restrict__ vo,
     const float2* __restrict__ grid, float2* __restrict__ cvr, int store,
-    double* __restrict__ part, int part_stride, uint32_t* __restrict__ cmax) {
+    double* __restrict__ part, int part_stride, uint32_t* __restrict__ cmax,
+    uint32_t* __restrict__ done, const int64_t* __restrict__ nvis, int normalize,
+    double* __restrict__ chi2_out) {
   const int c = blockIdx.y;
   float mx = 0.0f;
   const ChanRange rg = ranges[c];
@@ -210,33 +250,8 @@ __global__ void __launch_bounds__(256) k_degrid(
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = acc;
-}
-
-// Sum of channel partials in a fixed order; writes 0.5 * sum to out.
-__global__ void k_finish_chi2(int C, int nb, const double* __restrict__ part, int part_stride,
-                              const int64_t* __restrict__ nvis, int normalize,
-                              double* __restrict__ out) {
-  __shared__ double tot;
-  if (threadIdx.x == 0) tot = 0.0;
-  __syncthreads();
-  for (int c = 0; c < C; c++) {
-    double v = 0.0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[(int64_t)c * part_stride + b];
-    v = block_sum(v);
-    if (threadIdx.x == 0) {
-      if (normalize && nvis[c] > 0) v /= (double)nvis[c];
-      tot += v;
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *out = 0.5 * tot;
-}
-
-__global__ void k_finish_sum(int nb, const double* __restrict__ part, double* __restrict__ out) {
-  double v = 0.0;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += part[b];
-  v = block_sum(v);
-  if (threadIdx.x == 0) *out = v;
+  if (last_block_done(done, gridDim.x * gridDim.y))
+    finish_chi2(gridDim.y, gridDim.x, part, part_stride, nvis, normalize, chi2_out);
 }
 
 // ---- priors ---------------------------------------------------------------
@@ -353,9 +368,12 @@ __device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
   return 0.0f;
 }
 
+// prior value partials; the last block to finish sums them in a fixed order
 __global__ void __launch_bounds__(256) k_prior_value(PriorParams pp, const float* __restrict__ I,
                                                      const uint8_t* __restrict__ mask,
-                                                     double* __restrict__ part) {
+                                                     double* __restrict__ part,
+                                                     uint32_t* __restrict__ done,
+                                                     double* __restrict__ out) {
   double acc = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
        q += (int64_t)gridDim.x * blockDim.x) {
@@ -365,6 +383,12 @@ __global__ void __launch_bounds__(256) k_prior_value(PriorParams pp, const float
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  if (last_block_done(done, gridDim.x)) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(part + b);
+    v = block_sum(v);
+    if (threadIdx.x == 0) *out = v;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float* __restrict__ I,
@@ -381,10 +405,15 @@ __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float*
 
 }  // namespace
 
-static int cols_per_block(int n) {
+// Columns per block of the column pass: up to 16 (128-byte row segments,
+// 16K complex values of shared memory), fewer while the launch would have
+// under two blocks per SM (small images: 256^2 runs 256 one-column blocks
+// instead of 16 sixteen-column ones).
+static int cols_per_block(int n, int channels, int num_sms) {
   int cb = 16384 / n;
   if (cb < 1) cb = 1;
   if (cb > 16) cb = 16;
+  while (cb > 1 && (int64_t)(n / cb) * channels < 2 * (int64_t)num_sms) cb >>= 1;
   return cb;
 }
 
@@ -420,7 +449,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   k_rows_fft<<<dim3(n, C), threads, sm1, P.stream>>>(sp, P.d_chfreq, d_img, P.d_mask, P.d_twiddle,
                                                      P.d_grid);
   GV_LAUNCH("k_rows_fft");
-  const int cb = cols_per_block(n);
+  const int cb = cols_per_block(n, C, P.num_sms);
   const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n / 2);
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
@@ -444,11 +473,10 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
   if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
   k_degrid<<<dim3(nb, C), th, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
                                               P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride,
-                                              P.d_flags + kFlagCvrMax);
+                                              P.d_flags + kFlagCvrMax,
+                                              P.d_flags + kFlagDegridDone, P.d_chnvis,
+                                              P.normalize, P.d_scal + kSlotChi2);
   GV_LAUNCH("k_degrid");
-  k_finish_chi2<<<1, 256, 0, P.stream>>>(C, nb, P.d_part, P.part_stride, P.d_chnvis, P.normalize,
-                                         P.d_scal + kSlotChi2);
-  GV_LAUNCH("k_finish_chi2");
   return GV_OK;
 }
 
@@ -472,10 +500,9 @@ gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot) {
   const int64_t MN = pp.MN;
   int nb = (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
   double* part = P.d_part + (int64_t)P.part_stride * (P.chans.size() + t);
-  k_prior_value<<<nb, 256, 0, P.stream>>>(pp, d_img + MN * tm.image_index, P.d_mask, part);
+  k_prior_value<<<nb, 256, 0, P.stream>>>(pp, d_img + MN * tm.image_index, P.d_mask, part,
+                                          P.d_flags + kFlagPriorDone, P.d_scal + slot);
   GV_LAUNCH("k_prior_value");
-  k_finish_sum<<<1, 256, 0, P.stream>>>(nb, part, P.d_scal + slot);
-  GV_LAUNCH("k_finish_sum");
   return GV_OK;
 }
 
