@@ -43,6 +43,7 @@ enum FlagSlot {
   kFlagPsfMax = 3,    // max weight of a kept visibility (float bits)
   kFlagDegridDone = 4,  // blocks of k_degrid done (the last one finishes chi2)
   kFlagPriorDone = 5,   // blocks of k_prior_value done (the last one sums)
+  kFlagOptDone = 6,     // blocks of an optimiser reduction done (the last one sums)
   kNumFlags = 8
 };
 
@@ -197,6 +198,23 @@ __device__ inline float attenuation(int i, int j, float xobs, float yobs,
     }
   }
   return arc <= cutoff ? atten : 0.0f;
+}
+
+// True in every thread of the block that finishes last of `nblocks` (after
+// each block stored its partials); that block resets the counter for the
+// next launch.  It then combines the partials in a fixed order, so the
+// result does not depend on which block finished last.
+__device__ inline bool last_block_done(uint32_t* counter, uint32_t nblocks) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t prev = atomicAdd(counter, 1u);
+    last = prev == nblocks - 1 ? 1 : 0;
+    if (last) *counter = 0u;
+  }
+  __syncthreads();
+  return last != 0;
 }
 
 // ---- entry points between translation units ----------------------------

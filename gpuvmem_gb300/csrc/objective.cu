@@ -168,23 +168,6 @@ __device__ double block_sum(double v) {
   return v;
 }
 
-// True in every thread of the block that finishes last of `nblocks` (after
-// each block stored its partial); that block resets the counter for the next
-// launch.  The last block then sums the partials in a fixed order, so the
-// result does not depend on which block finished last.
-__device__ bool last_block_done(uint32_t* counter, uint32_t nblocks) {
-  __shared__ int last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const uint32_t prev = atomicAdd(counter, 1u);
-    last = prev == nblocks - 1 ? 1 : 0;
-    if (last) *counter = 0u;
-  }
-  __syncthreads();
-  return last != 0;
-}
-
 // Sum of channel partials in a fixed order; writes 0.5 * sum to out
 // (chi2(), src/functions.cu:4408-4451: per channel /V when normalize).
 __device__ void finish_chi2(int C, int nb, const double* part, int part_stride,

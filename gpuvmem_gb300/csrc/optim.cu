@@ -47,6 +47,32 @@ __device__ __forceinline__ float warp_max_f(float v) {
   return v;
 }
 
+// block-wide FP64 sum and max in a fixed order (result valid in thread 0)
+__device__ double block_sum_d(double v) {
+  __shared__ double sh[32];
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  return t;
+}
+__device__ double block_max_d(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = v;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, sh[w]);
+  return t;
+}
+
 // evaluateXt / evaluateXtNoPositivity, src/functions.cu:2832-2864
 __global__ void k_eval_xt(int64_t MN, float x, float floor_val, double floor_cmp,
                           int positivity, const float* __restrict__ pcom,
@@ -107,7 +133,9 @@ __global__ void __launch_bounds__(256) k_cg_stats(int64_t n, float den,
                                                   const float* __restrict__ xi,
                                                   const float* __restrict__ g,
                                                   const float* __restrict__ p,
-                                                  double* __restrict__ part, int stride) {
+                                                  double* __restrict__ part, int stride,
+                                                  uint32_t* __restrict__ done,
+                                                  double* __restrict__ out) {
   double gg = 0.0, dgg = 0.0;
   float gmax = FLT_MIN;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
@@ -141,26 +169,31 @@ __global__ void __launch_bounds__(256) k_cg_stats(int64_t n, float den,
     part[stride + blockIdx.x] = b;
     part[2 * stride + blockIdx.x] = (double)m;
   }
-}
-
-__global__ void k_cg_finish(int nb, const double* __restrict__ part, int stride,
-                            double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
-  double a = 0.0, b = 0.0, m = (double)FLT_MIN;
-  for (int i = 0; i < nb; i++) {
-    a += part[i];
-    b += part[stride + i];
-    m = fmax(m, part[2 * stride + i]);
+  if (last_block_done(done, gridDim.x)) {
+    // the block partials, each thread over a fixed stride, then the block
+    double a = 0.0, b = 0.0, m = (double)FLT_MIN;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      a += __ldcg(part + i);
+      b += __ldcg(part + stride + i);
+      m = fmax(m, __ldcg(part + 2 * stride + i));
+    }
+    a = block_sum_d(a);
+    b = block_sum_d(b);
+    m = block_max_d(m);
+    if (threadIdx.x == 0) {
+      out[0] = a;
+      out[1] = b;
+      out[2] = m;
+    }
   }
-  out[0] = a;
-  out[1] = b;
-  out[2] = m;
 }
 
 // FP64 dot product partials of two float vectors
 __global__ void __launch_bounds__(256) k_dot(int64_t n, const float* __restrict__ a,
                                              const float* __restrict__ b,
-                                             double* __restrict__ part) {
+                                             double* __restrict__ part,
+                                             uint32_t* __restrict__ done,
+                                             double* __restrict__ out) {
   double s = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x)
@@ -174,19 +207,19 @@ __global__ void __launch_bounds__(256) k_dot(int64_t n, const float* __restrict_
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
     part[blockIdx.x] = t;
   }
-}
-
-__global__ void k_sum_partials(int nb, const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x == 0) {
+  if (last_block_done(done, gridDim.x)) {
     double t = 0.0;
-    for (int i = 0; i < nb; i++) t += part[i];
-    *out = t;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += __ldcg(part + i);
+    t = block_sum_d(t);
+    if (threadIdx.x == 0) *out = t;
   }
 }
 
 // max |x| (normArray + deviceMaxReduce, seeded with FLT_MIN)
 __global__ void __launch_bounds__(256) k_absmax(int64_t n, const float* __restrict__ x,
-                                                double* __restrict__ part) {
+                                                double* __restrict__ part,
+                                                uint32_t* __restrict__ done,
+                                                double* __restrict__ out) {
   float m = FLT_MIN;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x)
@@ -200,13 +233,11 @@ __global__ void __launch_bounds__(256) k_absmax(int64_t n, const float* __restri
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmaxf(t, sh[w]);
     part[blockIdx.x] = (double)t;
   }
-}
-
-__global__ void k_max_partials(int nb, const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x == 0) {
+  if (last_block_done(done, gridDim.x)) {
     double t = (double)FLT_MIN;
-    for (int i = 0; i < nb; i++) t = fmax(t, part[i]);
-    *out = t;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t = fmax(t, __ldcg(part + i));
+    t = block_max_d(t);
+    if (threadIdx.x == 0) *out = t;
   }
 }
 
@@ -453,8 +484,8 @@ class Solver {
   gv_status dot(const float* a, const float* b, int64_t n, double* out) {
     const int nb = (int)std::min<int64_t>(nblk(n), P_.part_stride);
     double* part = P_.d_part;
-    k_dot<<<nb, 256, 0, P_.stream>>>(n, a, b, part);
-    k_sum_partials<<<1, 32, 0, P_.stream>>>(nb, part, P_.d_scal + kSlotOpt);
+    k_dot<<<nb, 256, 0, P_.stream>>>(n, a, b, part, P_.d_flags + kFlagOptDone,
+                                     P_.d_scal + kSlotOpt);
     GV_LAUNCH("k_dot");
     GV_TRY(fetch_scalars(P_, kSlotOpt + 1));
     *out = P_.h_scal[kSlotOpt];
@@ -463,8 +494,8 @@ class Solver {
 
   gv_status absmax(const float* x, int64_t n, float* out) {
     const int nb = (int)std::min<int64_t>(nblk(n), P_.part_stride);
-    k_absmax<<<nb, 256, 0, P_.stream>>>(n, x, P_.d_part);
-    k_max_partials<<<1, 32, 0, P_.stream>>>(nb, P_.d_part, P_.d_scal + kSlotOpt);
+    k_absmax<<<nb, 256, 0, P_.stream>>>(n, x, P_.d_part, P_.d_flags + kFlagOptDone,
+                                        P_.d_scal + kSlotOpt);
     GV_LAUNCH("k_absmax");
     GV_TRY(fetch_scalars(P_, kSlotOpt + 1));
     *out = (float)P_.h_scal[kSlotOpt];
@@ -495,8 +526,8 @@ class Solver {
       const float den = std::max(fp, 1.0f);
       const int nb = (int)std::min<int64_t>(nblk(PMN), P_.part_stride);
       k_cg_stats<<<nb, 256, 0, P_.stream>>>(PMN, den, w_.xi, w_.g, img, P_.d_part,
-                                             P_.part_stride);
-      k_cg_finish<<<1, 32, 0, P_.stream>>>(nb, P_.d_part, P_.part_stride, P_.d_scal + kSlotOpt);
+                                             P_.part_stride, P_.d_flags + kFlagOptDone,
+                                             P_.d_scal + kSlotOpt);
       GV_LAUNCH("k_cg_stats");
       GV_TRY(fetch_scalars(P_, kSlotOpt + 3));
       const float gg = (float)P_.h_scal[kSlotOpt], dgg = (float)P_.h_scal[kSlotOpt + 1];
