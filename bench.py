@@ -201,6 +201,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(t, dist, device):
+    """The slowest rank's time (every rank gets it).  Ranks are independent
+    replicas of the problem, so this is the whole job's time."""
+    import torch
+    tt = torch.tensor([float(t)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(world, steps, t):
+    """Whole-job evaluations per second of `world` replicas that each did
+    `steps` evaluations in (at most) t seconds."""
+    return world * steps / t
+
+
 def _gen_device():
     import torch
     return "cuda" if torch.cuda.is_available() else None
@@ -260,10 +275,8 @@ def run_ours(args):
     launches = (gv.launch_count() - launches0) // args.steps
     t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     if dist:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = world * args.steps / t
+        t = max_over_ranks(t, dist, "cuda")
+    value = replica_throughput(world, args.steps, t)
 
     # DChi2 kernel alone (for the roofline): gv_dchi2 = tcgen05 kernel +
     # split-K reduce
