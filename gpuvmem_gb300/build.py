@@ -26,6 +26,11 @@ def nvcc():
     return cand
 
 
+# per-file flags: the line-search controller rounds every float operation
+# separately, as the host code does
+FILE_FLAGS = {"linesearch.cu": ["-fmad=false"]}
+
+
 def sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
@@ -34,7 +39,8 @@ def _compile(src, extra):
     obj = os.path.join(OBJ, src + ".o")
     cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
-           "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj, *extra]
+           "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj, *FILE_FLAGS.get(src, []),
+           *extra]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -31,6 +31,7 @@ enum ScalarSlot {
   kSlotChi2 = 1,      // chi2 (0.5 * sum)
   kSlotTerm0 = 2,     // per-term values (up to kMaxTerms)
   kSlotOpt = 16,      // optimiser scratch (gg, dgg, gmax, dots ...)
+  kSlotLs = 40,       // device line search: fret, evaluations, error
   kNumScal = 64
 };
 constexpr int kMaxTerms = 8;
@@ -136,6 +137,8 @@ struct Problem {
   int degrid_threads = 256;      // k_degrid block size
   int degrid_blocks = 0;         // k_degrid blocks per channel cap (0: part_stride)
   void* graphs = nullptr;        // graph cache (graph.cu)
+  void* ls_graphs = nullptr;     // device line-search graphs (optim.cu)
+  struct LsState* d_ls = nullptr;  // device line-search state
 };
 
 // error state
@@ -217,6 +220,30 @@ __device__ inline bool last_block_done(uint32_t* counter, uint32_t nblocks) {
   return last != 0;
 }
 
+// ---- device line search (linesearch.cu) ---------------------------------
+// State of linmin's bracket + Brent search (src/linmin.cu:52-110,
+// src/mnbrak.cu:44-98, src/brent.cu:43-121) kept in device memory, advanced
+// by one thread after every objective evaluation.
+struct LsState {
+  int state, evals, steps, it, error, nterms, cap;
+  float ax, bx, cx, fa, fb, fc, u, fu;
+  float a, b, d, e, v, w, x, fv, fw, fx, tol;
+  float x_req;        // the point the next evaluation is at
+  float xmin, fret;   // the result
+  float lambda[kMaxTerms];
+};
+struct LsTerms {
+  int nterms;
+  float lambda[kMaxTerms];
+};
+// k_ls_begin: a new search from (0, 1) with tolerance tol; asks for f(0)
+gv_status ls_begin_launch(cudaStream_t st, LsState* s, LsTerms terms, float tol, int cap);
+// k_ls_step: takes f at x_req from the scalars the objective left, advances
+// the search to its next point or its end, and sets the graph's loop
+// condition (1: evaluate again, 0: done); at the end fret, the evaluation
+// count, the error flag and xmin go to scal[kSlotLs..kSlotLs+3]
+gv_status ls_step_launch(cudaStream_t st, LsState* s, double* scal, cudaGraphConditionalHandle h);
+
 // ---- entry points between translation units ----------------------------
 gv_status setup_problem(Problem& P, const gv_problem_desc& d);
 void free_problem(Problem& P);
@@ -246,6 +273,7 @@ gv_status check_device_error(Problem& P);
 gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt, int what,
                      bool store);
 void graph_cache_free(Problem& P);
+void ls_cache_free(Problem& P);
 
 // optimiser
 gv_status autotune(Problem& P, gv_tune_report* rep);

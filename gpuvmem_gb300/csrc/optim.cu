@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "gv_internal.cuh"
 
@@ -74,20 +75,25 @@ __device__ double block_max_d(double v) {
 }
 
 // evaluateXt / evaluateXtNoPositivity, src/functions.cu:2832-2864
-__global__ void k_eval_xt(int64_t MN, float x, float floor_val, double floor_cmp,
-                          int positivity, const float* __restrict__ pcom,
+// (x from x_dev when it is set: the device line search's point)
+__global__ void k_eval_xt(int64_t MN, float x, const float* __restrict__ x_dev, float floor_val,
+                          double floor_cmp, int positivity, const float* __restrict__ pcom,
                           const float* __restrict__ xicom, float* __restrict__ xt) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= 2 * MN) return;
+  if (x_dev) x = *x_dev;
   const float v = fmaf(x, xicom[q], pcom[q]);
   xt[q] = (q < MN && positivity && !((double)v > floor_cmp)) ? floor_val : v;
 }
 
 // newP / newPNoPositivity, src/functions.cu:2779-2812
-__global__ void k_new_p(int64_t MN, float xmin, float floor_val, double floor_cmp,
-                        int positivity, float* __restrict__ p, float* __restrict__ xi) {
+// (xmin from xmin_dev when it is set: the device line search's minimum)
+__global__ void k_new_p(int64_t MN, float xmin, const float* __restrict__ xmin_dev,
+                        float floor_val, double floor_cmp, int positivity, float* __restrict__ p,
+                        float* __restrict__ xi) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= 2 * MN) return;
+  if (xmin_dev) xmin = *xmin_dev;
   const float s = xi[q] * xmin;
   if (q < MN && positivity) {
     if ((double)(p[q] + s) > floor_cmp) {
@@ -278,6 +284,110 @@ struct Workspace {
   float *pcom, *xicom, *xt, *xi, *g, *h, *xi_old, *p_old, *q, *r;
 };
 
+// ---- device line search: one graph launch per linmin --------------------
+// Graph: k_ls_begin, then a WHILE node whose body evaluates the objective at
+// the controller's point (k_eval_xt, the objective kernels) and advances the
+// controller (k_ls_step), which ends the loop.  One graph per set of
+// buffers and objective gating, as for the evaluation graphs.
+constexpr int kLsCap = 4096;  // objective evaluations of one search at most
+
+struct LsEntry {
+  const float* pcom;
+  const float* xicom;
+  float* xt;
+  int flag, gate, positivity;
+  cudaGraphExec_t exec;
+  int64_t body_launches;
+  uint64_t stamp;
+};
+struct LsCache {
+  std::vector<LsEntry> e;
+  cudaStream_t cap = nullptr;
+  uint64_t clock = 0;
+};
+constexpr size_t kMaxLsGraphs = 4;
+
+LsCache& ls_cache(Problem& P) {
+  if (!P.ls_graphs) P.ls_graphs = new LsCache();
+  return *static_cast<LsCache*>(P.ls_graphs);
+}
+
+gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
+                         const float* xicom, float* xt, int flag, int positivity, float floor_val,
+                         double floor_cmp, const LsTerms& terms, cudaGraphExec_t* out,
+                         int64_t* body_launches) {
+  if (!c.cap) GV_CUDA(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
+  cudaGraph_t root = nullptr;
+  GV_CUDA(cudaGraphCreate(&root, 0));
+  struct Guard {
+    cudaGraph_t g;
+    ~Guard() {
+      if (g) cudaGraphDestroy(g);
+    }
+  } guard{root};
+  const int64_t l0 = gv_launch_count();
+  GV_CUDA(cudaStreamBeginCaptureToGraph(c.cap, root, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed));
+  gv_status s = ls_begin_launch(c.cap, P.d_ls, terms, 1.0e-7f, kLsCap);
+  cudaGraph_t g1 = root;
+  cudaError_t e = cudaStreamEndCapture(c.cap, &g1);
+  if (s != GV_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (line search start)");
+  cudaGraphNode_t begin = nullptr;
+  size_t nn = 1;
+  GV_CUDA(cudaGraphGetNodes(root, &begin, &nn));
+  if (nn != 1) {
+    set_error("line-search graph: unexpected start nodes");
+    return GV_ERR_CUDA;
+  }
+  cudaGraphConditionalHandle h;
+  GV_CUDA(cudaGraphConditionalHandleCreate(&h, root, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t loop = nullptr;
+  GV_CUDA(cudaGraphAddNode(&loop, root, &begin, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  const int64_t l1 = gv_launch_count();
+  const cudaStream_t saved = P.stream;
+  P.stream = c.cap;
+  e = cudaStreamBeginCaptureToGraph(c.cap, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    P.stream = saved;
+    return cuda_fail(e, "cudaStreamBeginCaptureToGraph (line search body)");
+  }
+  k_eval_xt<<<nblk(2 * MN), 256, 0, c.cap>>>(MN, 0.0f, &P.d_ls->x_req, floor_val, floor_cmp,
+                                               positivity, pcom, xicom, xt);
+  count_launch();
+  s = objective_launch(P, xt, flag, false);
+  if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
+  cudaGraph_t g2 = body;
+  e = cudaStreamEndCapture(c.cap, &g2);
+  P.stream = saved;
+  *body_launches = gv_launch_count() - l1;
+  add_launches(-(gv_launch_count() - l0));  // counted again at each replay
+  if (s != GV_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (line search body)");
+  GV_CUDA(cudaGraphInstantiate(out, root, 0));
+  return GV_OK;
+}
+
+}  // namespace
+
+void ls_cache_free(Problem& P) {
+  if (!P.ls_graphs) return;
+  LsCache* c = static_cast<LsCache*>(P.ls_graphs);
+  for (auto& g : c->e) cudaGraphExecDestroy(g.exec);
+  if (c->cap) cudaStreamDestroy(c->cap);
+  delete c;
+  P.ls_graphs = nullptr;
+}
+
+namespace {
+
 class Solver {
  public:
   Solver(Problem& P, const gv_opt_desc& o) : P_(P), o_(o) {
@@ -300,6 +410,11 @@ class Solver {
     w_ = Workspace{b, b + s, b + 2 * s, b + 3 * s, b + 4 * s, b + 5 * s,
                    b + 6 * s, b + 7 * s, b + 8 * s, b + 9 * s};
     GV_CUDA(cudaMemsetAsync(P_.d_opt, 0, need, P_.stream));
+    // the line search runs on the GPU inside a graph unless graphs are off
+    // or GV_DEVICE_LS=0
+    const char* dl = std::getenv("GV_DEVICE_LS");
+    dev_ls_ = P_.use_graphs && !(dl && std::atoi(dl) == 0) && P_.terms.size() <= (size_t)kMaxTerms;
+    if (dev_ls_ && !P_.d_ls) GV_CUDA(cudaMalloc(&P_.d_ls, sizeof(LsState)));
     if (o_.kind == GV_OPT_LBFGS) {
       const size_t ring = sizeof(float) * (size_t)MN_ * o_.K * 2;
       if (P_.lbfgs_bytes < 2 * ring) {
@@ -338,7 +453,7 @@ class Solver {
 
   // f1dim: xt = pcom + x*xicom (floored on plane 0), then the objective.
   gv_status f1dim(float x, float* out) {
-    k_eval_xt<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, x, floor_val_, floor_cmp_,
+    k_eval_xt<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, x, nullptr, floor_val_, floor_cmp_,
                                                      o_.positivity, w_.pcom, w_.xicom, w_.xt);
     GV_LAUNCH("k_eval_xt");
     return func(w_.xt, false, out);
@@ -467,15 +582,66 @@ class Solver {
     return GV_OK;
   }
 
+  // linmin on the GPU: the whole bracket + Brent search as one graph launch
+  gv_status linmin_device(float* p, float* xi, float* fret) {
+    LsCache& c = ls_cache(P_);
+    const int gate = P_.iteration > 0 ? 1 : 0;
+    LsEntry* hit = nullptr;
+    for (auto& g : c.e)
+      if (g.pcom == w_.pcom && g.xicom == w_.xicom && g.xt == w_.xt && g.flag == o_.flag &&
+          g.gate == gate && g.positivity == o_.positivity)
+        hit = &g;
+    if (!hit) {
+      LsTerms terms{};
+      terms.nterms = (int)P_.terms.size();
+      for (size_t t = 0; t < P_.terms.size(); t++) terms.lambda[t] = P_.terms[t].lambda;
+      cudaGraphExec_t exec = nullptr;
+      int64_t body = 0;
+      GV_TRY(build_ls_graph(P_, c, MN_, w_.pcom, w_.xicom, w_.xt, o_.flag, o_.positivity,
+                            floor_val_, floor_cmp_, terms, &exec, &body));
+      if (c.e.size() >= kMaxLsGraphs) {
+        auto old = std::min_element(c.e.begin(), c.e.end(), [](const LsEntry& a,
+                                                               const LsEntry& b) {
+          return a.stamp < b.stamp;
+        });
+        cudaGraphExecDestroy(old->exec);
+        c.e.erase(old);
+      }
+      c.e.push_back({w_.pcom, w_.xicom, w_.xt, o_.flag, gate, o_.positivity, exec, body, 0});
+      hit = &c.e.back();
+    }
+    hit->stamp = ++c.clock;
+    GV_CUDA(cudaMemcpyAsync(w_.pcom, p, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
+    GV_CUDA(cudaMemcpyAsync(w_.xicom, xi, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
+    GV_CUDA(cudaGraphLaunch(hit->exec, P_.stream));
+    k_new_p<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, 0.0f, &P_.d_ls->xmin, floor_val_,
+                                                   floor_cmp_, o_.positivity, p, xi);
+    GV_LAUNCH("k_new_p");
+    GV_TRY(fetch_scalars(P_, kSlotLs + 4));
+    const int64_t evals = (int64_t)P_.h_scal[kSlotLs + 1];
+    n_obj_ += evals;
+    add_launches(1 + evals * hit->body_launches);
+    *fret = (float)P_.h_scal[kSlotLs];
+    if (P_.h_scal[kSlotLs + 2] != 0.0) {
+      set_error("line search did not end within its evaluation limit (unbounded along the line?)");
+      return GV_ERR_DEVICE;
+    }
+    if (verbose())
+      std::fprintf(stderr, "Alpha for linear minimization = %.9g (f = %.9g)\n",
+                   (float)P_.h_scal[kSlotLs + 3], *fret);
+    return GV_OK;
+  }
+
   // linmin, src/linmin.cu:52-110
   gv_status linmin(float* p, float* xi, float* fret) {
+    if (dev_ls_) return linmin_device(p, xi, fret);
     GV_CUDA(cudaMemcpyAsync(w_.pcom, p, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
     GV_CUDA(cudaMemcpyAsync(w_.xicom, xi, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
     float ax = 0.0f, xx = 1.0f, bx, fa, fx, fb, xmin;
     GV_TRY(bracket(&ax, &xx, &bx, &fa, &fx, &fb));
     GV_TRY(brent(ax, xx, bx, 1.0e-7f, &xmin, fret));
     if (verbose()) std::fprintf(stderr, "Alpha for linear minimization = %.9g (f = %.9g)\n", xmin, *fret);
-    k_new_p<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, xmin, floor_val_, floor_cmp_,
+    k_new_p<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, xmin, nullptr, floor_val_, floor_cmp_,
                                                    o_.positivity, p, xi);
     GV_LAUNCH("k_new_p");
     return GV_OK;
@@ -635,6 +801,7 @@ class Solver {
   }
 
   int64_t n_obj_ = 0, n_grad_ = 0;
+  bool dev_ls_ = false;  // line search on the GPU (one graph launch per linmin)
   // stop once a line search reaches this value (priors active, i.e. from
   // the second iteration on); -inf: never
   double f_target_ = -INFINITY;

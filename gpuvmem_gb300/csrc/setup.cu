@@ -197,6 +197,8 @@ void free_problem(Problem& P) {
   cudaFree(P.tc_partial);
   if (P.h_scal) cudaFreeHost(P.h_scal);
   graph_cache_free(P);
+  ls_cache_free(P);
+  cudaFree(P.d_ls);
   P = Problem();
 }
 
