@@ -120,6 +120,8 @@ struct Problem {
   size_t opt_bytes = 0;
   float* d_lbfgs = nullptr;      // L-BFGS s/y rings
   size_t lbfgs_bytes = 0;
+  void* d_lbscal = nullptr;      // L-BFGS recursion scalars (FP64 dots, float alphas)
+  size_t lbscal_bytes = 0;
   float* d_chfreq = nullptr;     // [C] channel frequencies
   ChanRange* d_ranges = nullptr; // [C] kept-visibility ranges
   int64_t* d_chnvis = nullptr;   // [C] visibilities per channel (normalize)

@@ -265,6 +265,56 @@ __global__ void k_scaled_copy(int64_t n, float s, const float* __restrict__ q,
   if (k < n) r[k] = q[k] * s;
 }
 
+// The L-BFGS recursion with its scalars kept on the device: the dot
+// products land in FP64 device scalars and these kernels form rho, alpha
+// and beta from them with the host recursion's float operations, each
+// rounded on its own (no contraction into FMAs, as the host code is
+// compiled), so nothing is read back per dot product and the result is the
+// host recursion's bit for bit.
+//   first loop:  rho = 1 / (float)y.s (in double, then float), alpha =
+//                rho (float)s.q, q -= alpha y
+//   second loop: rho = 1.0f / (float)y.s, beta = rho (float)y.r,
+//                r += (alpha - beta) s
+__global__ void k_lbfgs_axpy(int64_t n, int second, const double* __restrict__ d1,
+                             const double* __restrict__ d2, float* __restrict__ alpha,
+                             const float* __restrict__ x, float* __restrict__ y) {
+  __shared__ float coef_s;
+  if (threadIdx.x == 0) {
+    const float rho_den = (float)*d1;
+    if (!second) {
+      const float rho = rho_den != 0.0f ? (float)__ddiv_rn(1.0, (double)rho_den) : 0.0f;
+      const float a = __fmul_rn(rho, (float)*d2);
+      coef_s = -a;
+      if (blockIdx.x == 0) *alpha = a;
+    } else {
+      const float rho = rho_den != 0.0f ? __fdiv_rn(1.0f, rho_den) : 0.0f;
+      const float beta = __fmul_rn(rho, (float)*d2);
+      coef_s = __fsub_rn(*alpha, beta);
+    }
+  }
+  __syncthreads();
+  const float coef = coef_s;
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < n) y[q] = fmaf(coef, x[q], y[q]);
+}
+
+// H0 scale: sum over planes of (float)s.y / (float)y.y where y.y != 0
+__global__ void k_lbfgs_h0(const double* __restrict__ sy, const double* __restrict__ yy,
+                           float* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  float s = 0.0f;
+  for (int im = 0; im < 2; im++)
+    if ((float)yy[im] != 0.0f) s = __fadd_rn(s, __fdiv_rn((float)sy[im], (float)yy[im]));
+  *out = s;
+}
+
+// r := q * (*s)  (getR with the scale on the device)
+__global__ void k_scaled_copy_dev(int64_t n, const float* __restrict__ s,
+                                  const float* __restrict__ q, float* __restrict__ r) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) r[k] = __fmul_rn(q[k], *s);
+}
+
 // calculateSandY for one plane, src/functions.cu:3635
 __global__ void k_s_and_y(int64_t n, const float* __restrict__ xi, const float* __restrict__ xi_old,
                           const float* __restrict__ p, const float* __restrict__ p_old,
@@ -427,6 +477,23 @@ class Solver {
       d_y_ = P_.d_lbfgs;
       d_s_ = P_.d_lbfgs + (size_t)MN_ * o_.K * 2;
       GV_CUDA(cudaMemsetAsync(P_.d_lbfgs, 0, 2 * ring, P_.stream));
+      // device scalars of the recursion (GV_DEVICE_LBFGS=0: host scalars)
+      const char* dv = std::getenv("GV_DEVICE_LBFGS");
+      dev_lb_ = !(dv && std::atoi(dv) == 0);
+      const size_t sc_bytes = sizeof(double) * (4 * (size_t)o_.K + 4) +
+                              sizeof(float) * (2 * (size_t)o_.K + 1);
+      if (dev_lb_ && P_.lbscal_bytes < sc_bytes) {
+        cudaFree(P_.d_lbscal);
+        P_.d_lbscal = nullptr;
+        P_.lbscal_bytes = 0;
+        GV_CUDA(cudaMalloc(&P_.d_lbscal, sc_bytes));
+        P_.lbscal_bytes = sc_bytes;
+      }
+      if (dev_lb_) {
+        lb_sc_ = reinterpret_cast<double*>(P_.d_lbscal);
+        lb_f_ = reinterpret_cast<float*>(lb_sc_ + 4 * (size_t)o_.K + 4);
+        GV_CUDA(cudaMemsetAsync(P_.d_lbscal, 0, sc_bytes, P_.stream));
+      }
     }
     return GV_OK;
   }
@@ -757,6 +824,10 @@ class Solver {
       // LBFGS_recursion
       const int par_M = std::min(K, it);
       GV_CUDA(cudaMemcpyAsync(w_.q, w_.xi, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
+      if (dev_lb_) {
+        GV_TRY(lbfgs_recursion_device(par_M, lit));
+        continue;
+      }
       std::fill(alpha.begin(), alpha.end(), 0.0f);
       for (int im = 0; im < 2; im++) {
         for (int k = par_M - 1; k >= 0; k--) {
@@ -800,8 +871,66 @@ class Solver {
     return GV_OK;
   }
 
+  // LBFGS_recursion (src/lbfgs.cu:202-341) with the scalars on the device:
+  // the same kernels and dot products in the same order as the host
+  // version, no read-back per dot product
+  gv_status lbfgs_recursion_device(int par_M, int lit) {
+    const int K = o_.K;
+    auto slot = [&](float* base, int im, int k) { return base + MN_ * im * k + MN_ * im; };
+    auto qslot = [&](float* base, int im, int k) { return base + MN_ * im + MN_ * k; };
+    double* d1 = lb_sc_;          // [2K] y.s per plane and pair
+    double* d2 = lb_sc_ + 2 * K;  // [2K] s.q, then y.r
+    double* syy = lb_sc_ + 4 * K; // [4] s.y and y.y of the newest pair, per plane
+    float* alpha = lb_f_;         // [2K]
+    float* h0 = lb_f_ + 2 * K;    // [1]
+    const unsigned nb1 = nblk(MN_);
+    for (int im = 0; im < 2; im++) {
+      for (int k = par_M - 1; k >= 0; k--) {
+        GV_TRY(dot_to(slot(d_y_, im, k), slot(d_s_, im, k), MN_, d1 + im * K + k));
+        GV_TRY(dot_to(slot(d_s_, im, k), w_.q + MN_ * im, MN_, d2 + im * K + k));
+        k_lbfgs_axpy<<<nb1, 256, 0, P_.stream>>>(MN_, 0, d1 + im * K + k, d2 + im * K + k,
+                                                 alpha + im * K + k, qslot(d_y_, im, k),
+                                                 w_.q + MN_ * im);
+        GV_LAUNCH("k_lbfgs_axpy");
+      }
+    }
+    for (int im = 0; im < 2; im++) {
+      GV_TRY(dot_to(slot(d_y_, im, lit), slot(d_s_, im, lit), MN_, syy + im));
+      GV_TRY(dot_to(slot(d_y_, im, lit), slot(d_y_, im, lit), MN_, syy + 2 + im));
+    }
+    k_lbfgs_h0<<<1, 32, 0, P_.stream>>>(syy, syy + 2, h0);
+    GV_LAUNCH("k_lbfgs_h0");
+    for (int im = 0; im < 2; im++) {
+      k_scaled_copy_dev<<<nb1, 256, 0, P_.stream>>>(MN_, h0, w_.q + MN_ * im, w_.r + MN_ * im);
+      GV_LAUNCH("k_scaled_copy_dev");
+      for (int k = 0; k < par_M; k++) {
+        GV_TRY(dot_to(slot(d_y_, im, k), slot(d_s_, im, k), MN_, d1 + im * K + k));
+        GV_TRY(dot_to(slot(d_y_, im, k), w_.r + MN_ * im, MN_, d2 + im * K + k));
+        k_lbfgs_axpy<<<nb1, 256, 0, P_.stream>>>(MN_, 1, d1 + im * K + k, d2 + im * K + k,
+                                                 alpha + im * K + k, qslot(d_s_, im, k),
+                                                 w_.r + MN_ * im);
+        GV_LAUNCH("k_lbfgs_axpy");
+      }
+    }
+    const int64_t PMN = 2 * MN_;
+    k_scaled_copy<<<nblk(PMN), 256, 0, P_.stream>>>(PMN, -1.0f, w_.r, w_.xi);
+    GV_LAUNCH("k_scaled_copy");
+    return GV_OK;
+  }
+
+  // FP64 dot product into a device scalar (no read-back)
+  gv_status dot_to(const float* a, const float* b, int64_t n, double* out) {
+    const int nb = (int)std::min<int64_t>(nblk(n), P_.part_stride);
+    k_dot<<<nb, 256, 0, P_.stream>>>(n, a, b, P_.d_part, P_.d_flags + kFlagOptDone, out);
+    GV_LAUNCH("k_dot");
+    return GV_OK;
+  }
+
   int64_t n_obj_ = 0, n_grad_ = 0;
   bool dev_ls_ = false;  // line search on the GPU (one graph launch per linmin)
+  bool dev_lb_ = false;  // L-BFGS recursion scalars on the GPU
+  double* lb_sc_ = nullptr;
+  float* lb_f_ = nullptr;
   // stop once a line search reaches this value (priors active, i.e. from
   // the second iteration on); -inf: never
   double f_target_ = -INFINITY;

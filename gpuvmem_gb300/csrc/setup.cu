@@ -199,6 +199,7 @@ void free_problem(Problem& P) {
   graph_cache_free(P);
   ls_cache_free(P);
   cudaFree(P.d_ls);
+  cudaFree(P.d_lbscal);
   P = Problem();
 }
 

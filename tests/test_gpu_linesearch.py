@@ -1,7 +1,8 @@
 """The line search on the GPU (bracket + Brent as a state machine inside a
-CUDA-graph WHILE loop, one graph launch per linmin) against the host line
-search: the same points are visited, so iterations, evaluation counts, the
-final objective and the image agree bit for bit."""
+CUDA-graph WHILE loop, one graph launch per linmin) and the L-BFGS recursion
+with its scalars on the GPU, against the host versions: the same points and
+the same scalars, so iterations, evaluation counts, the final objective and
+the image agree bit for bit."""
 
 import os
 
@@ -13,10 +14,11 @@ from gpuvmem_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _solve(device_ls, method, iterations, seed, n=64, nchan=1):
+def _solve(device_ls, method, iterations, seed, n=64, nchan=1, device_lbfgs=True):
     import torch
     import gpuvmem_gb300 as gv
     os.environ["GV_DEVICE_LS"] = "1" if device_ls else "0"
+    os.environ["GV_DEVICE_LBFGS"] = "1" if device_lbfgs else "0"
     try:
         data = synth.generate(synth.small_config(n=n, nchan=nchan, seed=seed), device="cuda")
         prob = gv.Problem(data, [gv.term("Chi2", 1.0), gv.term("Entropy", 0.01),
@@ -27,6 +29,7 @@ def _solve(device_ls, method, iterations, seed, n=64, nchan=1):
         return rep, img.cpu().numpy()
     finally:
         os.environ.pop("GV_DEVICE_LS", None)
+        os.environ.pop("GV_DEVICE_LBFGS", None)
 
 
 @pytest.mark.parametrize("method,iterations", [("CG-FRPRMN", 15), ("CG-LBFGS", 10)])
@@ -43,4 +46,13 @@ def test_device_line_search_two_channels_128():
     rh, ih = _solve(False, "CG-FRPRMN", 8, seed=5, n=128, nchan=2)
     rd, idv = _solve(True, "CG-FRPRMN", 8, seed=5, n=128, nchan=2)
     assert rd.n_objective == rh.n_objective
+    np.testing.assert_array_equal(idv.view(np.uint32), ih.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_device_lbfgs_recursion_matches_host(n):
+    rh, ih = _solve(True, "CG-LBFGS", 12, seed=23, n=n, device_lbfgs=False)
+    rd, idv = _solve(True, "CG-LBFGS", 12, seed=23, n=n, device_lbfgs=True)
+    assert rd.iterations == rh.iterations and rd.n_objective == rh.n_objective
+    assert np.float32(rd.f_final).tobytes() == np.float32(rh.f_final).tobytes()
     np.testing.assert_array_equal(idv.view(np.uint32), ih.view(np.uint32))
