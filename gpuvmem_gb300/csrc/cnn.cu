@@ -178,7 +178,9 @@ struct View {
   int C, c0;
 };
 
-// forward: y = act(conv(x) + bias)
+// forward: y = act(conv(x) + bias); with split-K (part set) each split
+// stores its partial sum to part[split][n][m] and k_conv_fwd_finish adds
+// the splits, the bias and the activation
 struct ConvFwdOp {
   const float* x;
   int xC, xc0;
@@ -187,6 +189,8 @@ struct ConvFwdOp {
   float* y;
   int yC, yc0;
   int Cin, Cout, H, W, ks, relu;
+  float* part;
+  int M;
   __device__ float a(int m, int k) const {
     const int HW = H * W;
     const int b = m / HW, r = m - b * HW, y0 = r / W, x0 = r - y0 * W;
@@ -196,7 +200,11 @@ struct ConvFwdOp {
     return x[((size_t)(b * xC + xc0 + cin) * H + yy) * W + xx];
   }
   __device__ float b(int k, int n) const { return w[(size_t)n * Cin * ks * ks + k]; }
-  __device__ void store(int m, int n, float v, int) const {
+  __device__ void store(int m, int n, float v, int split) const {
+    if (part) {
+      part[((size_t)split * Cout + n) * M + m] = v;
+      return;
+    }
     const int HW = H * W;
     const int b = m / HW, r = m - b * HW;
     v += bias[n];
@@ -204,6 +212,21 @@ struct ConvFwdOp {
     y[(size_t)(b * yC + yc0 + n) * HW + r] = v;
   }
 };
+
+// split-K forward: y = act(sum over splits in order + bias)
+__global__ void k_conv_fwd_finish(int M, int N, int nsplit, const float* __restrict__ part,
+                                  const float* __restrict__ bias, int relu, float* __restrict__ y,
+                                  int yC, int yc0, int HW) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)M * N) return;
+  const int n = (int)(i / M), m = (int)(i - (size_t)n * M);
+  float s = 0.0f;
+  for (int k = 0; k < nsplit; k++) s += part[((size_t)k * N + n) * M + m];
+  s += bias[n];
+  if (relu) s = fmaxf(s, 0.0f);
+  const int b = m / HW, r = m - b * HW;
+  y[(size_t)(b * yC + yc0 + n) * HW + r] = s;
+}
 
 // backward data: dx (+)= conv of dz with the taps flipped
 struct ConvBwdDataOp {
@@ -434,8 +457,27 @@ inline int ew_blocks(size_t n, const Ctx& c) {
 
 gv_status conv_forward(const Ctx& c, View x, const float* w, const float* bias, View y, int B,
                        int Cin, int Cout, int H, int W, int ks, int relu) {
-  ConvFwdOp op{x.p, x.C, x.c0, w, bias, y.p, y.C, y.c0, Cin, Cout, H, W, ks, relu};
-  return launch_gemm(c, op, B * H * W, Cout, Cin * ks * ks);
+  const int M = B * H * W, N = Cout, K = Cin * ks * ks;
+  // a grid of fewer tiles than SMs (deep levels, small batches) splits K
+  // over up to two CTAs per SM, at least two K blocks a split
+  const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
+  const int tiles = ((M + kBM - 1) / kBM) * ((N + bn - 1) / bn);
+  int nsplit = 1;
+  if (c.part && tiles < c.num_sms) {
+    nsplit = std::min(K / (2 * kBK), (2 * c.num_sms + tiles - 1) / tiles);
+    nsplit = std::max(1, std::min<int>(nsplit, (int)(c.part_floats / ((size_t)M * N))));
+  }
+  ConvFwdOp op{x.p, x.C, x.c0, w, bias, y.p, y.C, y.c0, Cin, Cout, H, W, ks, relu,
+               nsplit > 1 ? c.part : nullptr, M};
+  gv_status s = launch_gemm(c, op, M, N, K, nsplit);
+  if (s != GV_OK || nsplit <= 1) return s;
+  // the kernel launched ceil(K / klen) splits; sum exactly those
+  const int klen = ((K + nsplit - 1) / nsplit + kBK - 1) / kBK * kBK;
+  const int nz = (K + klen - 1) / klen;
+  k_conv_fwd_finish<<<(unsigned)(((size_t)M * N + 255) / 256), 256, 0, c.stream>>>(
+      M, N, nz, c.part, bias, relu, y.p, y.C, y.c0, H * W);
+  GV_LAUNCH("k_conv_fwd_finish");
+  return GV_OK;
 }
 
 gv_status conv_backward_data(const Ctx& c, View dz, const float* w, View dx, int B, int Cin,

@@ -138,20 +138,22 @@ def choose_start(sky: Sky, net: UNet, scales=SCALES, cuts=CUTS):
     pixels below a fraction of its peak set to the floor (the factor and the
     fraction the objective prefers), if the objective, priors active, scores
     it at least as well as the plain start; else the plain start."""
+    import torch
     warm = warm_image(sky, net)
     plain = sky.prob.initial_image()
     sky.prob.set_iteration(1)
-    best, fw = None, float("inf")
     ex = warm[0] - sky.floor
-    peak = float(ex.max())
-    for cut in cuts:
-        kept = ex * (ex > cut * peak)
-        for a in scales:
-            cand = warm.clone()
-            cand[0] = sky.floor + a * kept
-            f, _ = sky.prob.objective(cand.clone())
-            if f < fw:
-                best, fw = cand, f
+    # every (cut, scale) candidate in one tensor, cut-major
+    cut_t = torch.tensor(cuts, dtype=ex.dtype, device=ex.device).view(-1, 1, 1)
+    kept = ex[None] * (ex[None] > cut_t * ex.max())                    # [cuts, H, W]
+    sc = torch.tensor(scales, dtype=ex.dtype, device=ex.device).view(1, -1, 1, 1)
+    cands = warm[None, None].repeat(len(cuts), len(scales), 1, 1, 1)    # [cuts, scales, 2, H, W]
+    cands[:, :, 0] = sky.floor + sc * kept[:, None]
+    flat = cands.view(-1, *warm.shape)
+    work = flat.clone()  # the objective clips the image it evaluates
+    fs = [sky.prob.objective(work[i])[0] for i in range(flat.shape[0])]
+    i_best = min(range(len(fs)), key=lambda i: (fs[i] if fs[i] == fs[i] else float("inf"), i))
+    best, fw = flat[i_best].clone(), fs[i_best]
     fp, _ = sky.prob.objective(plain.clone())
     sky.prob.set_iteration(0)
     return (best, "warm", fw, fp) if fw <= fp else (plain, "plain", fw, fp)
