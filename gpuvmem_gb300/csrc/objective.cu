@@ -14,7 +14,9 @@
 //
 // No per-call allocation, no host synchronisation except the single scalar
 // read-back at the end of an evaluation.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "gv_internal.cuh"
 
@@ -394,6 +396,7 @@ __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float*
 // instead of 16 sixteen-column ones).
 static int cols_per_block(int n, int channels, int num_sms) {
   int cb = 16384 / n;
+  if (const char* e = std::getenv("GV_FFT_CB_DIV")) cb /= std::max(1, std::atoi(e));
   if (cb < 1) cb = 1;
   if (cb > 16) cb = 16;
   while (cb > 1 && (int64_t)(n / cb) * channels < 2 * (int64_t)num_sms) cb >>= 1;
