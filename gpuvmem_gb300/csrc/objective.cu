@@ -390,13 +390,12 @@ __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float*
 
 }  // namespace
 
-// Columns per block of the column pass: up to 16 (128-byte row segments,
-// 16K complex values of shared memory), fewer while the launch would have
-// under two blocks per SM (small images: 256^2 runs 256 one-column blocks
-// instead of 16 sixteen-column ones).
+// Columns per block of the column pass: 4096 / n (4K complex values of
+// shared memory, so several blocks share an SM: 2 columns at 2048^2 measured
+// 1.4x faster than 8), fewer while the launch would have under two blocks per
+// SM (small images: 256^2 runs 256 one-column blocks).
 static int cols_per_block(int n, int channels, int num_sms) {
-  int cb = 16384 / n;
-  if (const char* e = std::getenv("GV_FFT_CB_DIV")) cb /= std::max(1, std::atoi(e));
+  int cb = 4096 / n;
   if (cb < 1) cb = 1;
   if (cb > 16) cb = 16;
   while (cb > 1 && (int64_t)(n / cb) * channels < 2 * (int64_t)num_sms) cb >>= 1;
