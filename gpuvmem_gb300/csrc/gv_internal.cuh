@@ -110,7 +110,7 @@ struct Problem {
   uint8_t* d_mask = nullptr;     // [MN]
   float* d_rho = nullptr;        // [MN] z - 1 + r^2/2 per pixel
   float2* d_grid = nullptr;      // [C][MN] model grids
-  float2* d_twiddle = nullptr;   // [n/2] e^{+2 pi i k/n}
+  float2* d_twiddle = nullptr;   // [n-1] e^{+2 pi i k/n}, stage-major (objective.cu smem_fft)
   double* d_part = nullptr;      // reduction partials
   int part_stride = 0;           // partials per channel / term
   double* d_scal = nullptr;      // [kNumScal]

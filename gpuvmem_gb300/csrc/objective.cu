@@ -34,13 +34,15 @@ __device__ __forceinline__ unsigned bitrev(unsigned x, int bits) {
 
 // In-place inverse radix-2 DIT FFT of `ncol` independent columns of length
 // n = 2^log2n held in shared memory (column c at buf + c*n), input in
-// bit-reversed order, output in natural order.
+// bit-reversed order, output in natural order.  tw is the stage-major
+// twiddle table (stage s at offset 2^(s-1) - 1), so the lanes of a warp read
+// consecutive twiddles instead of a power-of-two stride (bank conflicts).
 __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restrict__ tw) {
   const int n = 1 << log2n;
   const int nb = (n >> 1) * ncol;
   for (int s = 1; s <= log2n; s++) {
     const int half = 1 << (s - 1);
-    const int tstride = n >> s;
+    const float2* __restrict__ tws = tw + (half - 1);
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       const int col = b >> (log2n - 1);
       const int bb = b & ((n >> 1) - 1);
@@ -48,7 +50,7 @@ __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restr
       const int pos = bb & (half - 1);
       const int a0 = col * n + (grp << s) + pos;
       const int a1 = a0 + half;
-      const float2 w = tw[pos * tstride];
+      const float2 w = tws[pos];
       const float2 t = cmul(w, buf[a1]);
       const float2 x0 = buf[a0];
       buf[a0] = make_float2(x0.x + t.x, x0.y + t.y);
@@ -80,7 +82,7 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
   float2* tw = sm + n;
   const int i = blockIdx.x;
   const int c = blockIdx.y;
-  for (int k = threadIdx.x; k < n / 2; k += blockDim.x) tw[k] = tw_g[k];
+  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
   const float freq = chfreq[c];
   const float nudiv = freq / sp.nu_0;
   const float floor_inu = -1.0f * sp.eta * sp.minpix;
@@ -129,7 +131,7 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, float xphs, flo
   float2* tw = sm + (size_t)cb * n;
   const int j0 = blockIdx.x * cb;
   float2* G = grid + (int64_t)blockIdx.y * MN;
-  for (int k = threadIdx.x; k < n / 2; k += blockDim.x) tw[k] = tw_g[k];
+  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
     buf[cc * n + bitrev(r, log2n)] = G[(int64_t)n * r + j0 + cc];
@@ -428,14 +430,14 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.write_clip = write_clip;
   sp.gcf = P.d_gcf;
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
-  const size_t sm1 = sizeof(float2) * (n + n / 2);
+  const size_t sm1 = sizeof(float2) * (2 * n - 1);
   if (sm1 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_rows_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
   k_rows_fft<<<dim3(n, C), threads, sm1, P.stream>>>(sp, P.d_chfreq, d_img, P.d_mask, P.d_twiddle,
                                                      P.d_grid);
   GV_LAUNCH("k_rows_fft");
   const int cb = cols_per_block(n, C, P.num_sms);
-  const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n / 2);
+  const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n - 1);
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
   k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.xobs, P.yobs,

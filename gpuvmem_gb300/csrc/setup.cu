@@ -502,13 +502,18 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
 
   // ---- FFT twiddles, grids, reduction scratch -----------------------------
   {
-    std::vector<float2> tw(n / 2);
-    for (int k = 0; k < n / 2; k++) {
-      const double a = 2.0 * kPiD * k / n;
-      tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    // stage-major: stage s (half = 2^(s-1)) holds e^{+2 pi i pos (n >> s) / n}
+    // for pos < half at offset half - 1, so a stage reads consecutive entries
+    std::vector<float2> tw(n - 1);
+    for (int half = 1; half < n; half <<= 1) {
+      const int tstride = n / (2 * half);
+      for (int pos = 0; pos < half; pos++) {
+        const double a = 2.0 * kPiD * (pos * tstride) / n;
+        tw[half - 1 + pos] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
     }
-    GV_CUDA(cudaMalloc(&P.d_twiddle, sizeof(float2) * (n / 2)));
-    GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * (n / 2),
+    GV_CUDA(cudaMalloc(&P.d_twiddle, sizeof(float2) * (n - 1)));
+    GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * (n - 1),
                             cudaMemcpyHostToDevice, st));
   }
   GV_CUDA(cudaMalloc(&P.d_grid, sizeof(float2) * MN * C));
