@@ -468,8 +468,10 @@ def run_case(name, reps):
     recorded in profiles/): `dchi2_2048_1ch` (configuration 1 reduced to one
     channel at 230 GHz, natural weights, 16 s integrations), `cfg0`, and
     `weighting` (Uniform and Briggs weighting of configuration 1's 35.28M
-    visibilities on a 2048^2 grid) and `gridding` (the same visibilities
-    gridded with the PillBox2D and 7 x 7 PSWF kernels)."""
+    visibilities on a 2048^2 grid), `gridding` (the same visibilities
+    gridded with the PillBox2D and 7 x 7 PSWF kernels), `objective_cfg1`
+    (two objective evaluations of configuration 1) and
+    `objective_lbfgs_cfg1` (the same, then two L-BFGS iterations)."""
     import dataclasses
     import torch
     import gpuvmem_gb300 as gv
@@ -508,6 +510,24 @@ def run_case(name, reps):
                          "gridded_visibilities": int(res[0][-1])}
         print(json.dumps({"case": name, "visibilities": int(off[-1]), "grid": cfg.n,
                           "channels": len(freqs), "kernels": out}))
+        return
+    if name in ("objective_cfg1", "objective_lbfgs_cfg1"):
+        # configuration 1 with chi2 + entropy + TSV: two objective evaluations
+        # (priors on), then (second case) two L-BFGS iterations
+        data = synth.generate(synth.CONFIG1, device="cuda")
+        prob = gv.Problem(data, [gv.term("Chi2", 1.0), gv.term("Entropy", 0.01),
+                                 gv.term("TotalSquaredVariation", 1e-4)])
+        img = prob.initial_image()
+        prob.set_iteration(1)
+        for _ in range(2):
+            prob.objective(img)
+        rep = None
+        if name == "objective_lbfgs_cfg1":
+            prob.set_iteration(0)
+            rep = prob.optimize(img, "CG-LBFGS", iterations=2)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": name, "visibilities": int(data.nvis),
+                          "lbfgs_objective_evaluations": None if rep is None else int(rep.n_objective)}))
         return
     if name == "dchi2_2048_1ch":
         cfg = dataclasses.replace(synth.CONFIG1, freqs_hz=[230e9], weighting="natural", dt_s=16.0)
