@@ -251,10 +251,24 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d);
 void free_problem(Problem& P);
 
 // objective.cu
-gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+// A line-search point as the objective's input: xt = pcom + (*x_dev) xicom,
+// plane 0 floored at floor_val (positivity), evaluateXt of
+// src/functions.cu:2832-2864, formed inside the FFT staging (which writes xt)
+struct XtSource {
+  const float* pcom;
+  const float* xicom;
+  const float* x_dev;
+  float floor_val;
+  double floor_cmp;
+  int positivity;
+};
+gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                      const XtSource* xs = nullptr, double* term_out = nullptr,
+                      uint32_t zero_terms = 0u);
 gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot);
 gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi);
-gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                           const XtSource* xs = nullptr);
 gv_status fetch_scalars(Problem& P, int n);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);

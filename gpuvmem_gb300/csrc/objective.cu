@@ -70,6 +70,7 @@ struct StageParams {
   int flag_opt;
   int write_clip;
   const float* gcf;  // gridding correction, or null
+  XtSource xs;       // xs.pcom set: the image is xt = pcom + x xicom (written back)
 };
 
 // Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
@@ -88,22 +89,36 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
   const float floor_inu = -1.0f * sp.eta * sp.minpix;
   const float clip_i0 = sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix);
   const bool writer = sp.write_clip && c == 0;
+  const bool from_xt = sp.xs.pcom != nullptr;
+  const float x = from_xt ? *sp.xs.x_dev : 0.0f;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const int64_t q = (int64_t)n * i + j;
-    float i0 = img[q];
-    float al = img[sp.MN + q];
+    float i0, al;
+    if (from_xt) {
+      // evaluateXt (k_eval_xt's arithmetic): plane 0 floored, plane 1 free
+      const float v0 = fmaf(x, sp.xs.xicom[q], sp.xs.pcom[q]);
+      i0 = (sp.xs.positivity && !((double)v0 > sp.xs.floor_cmp)) ? sp.xs.floor_val : v0;
+      al = fmaf(x, sp.xs.xicom[sp.MN + q], sp.xs.pcom[sp.MN + q]);
+    } else {
+      i0 = img[q];
+      al = img[sp.MN + q];
+    }
     const uint8_t m = mask[q];
     // clip2IWNoise, src/functions.cu:2694-2719 (mutates the image)
     if (m & kMaskClip) {
-      if (writer && (i0 != clip_i0 || al != 0.0f)) {
+      if (writer && !from_xt && (i0 != clip_i0 || al != 0.0f)) {
         img[q] = clip_i0;
         img[sp.MN + q] = 0.0f;
       }
       i0 = clip_i0;
       al = 0.0f;
     } else if (i0 < sp.threshold && sp.flag_opt > 0) {
-      if (writer && al != 0.0f) img[sp.MN + q] = 0.0f;
+      if (writer && !from_xt && al != 0.0f) img[sp.MN + q] = 0.0f;
       al = 0.0f;
+    }
+    if (writer && from_xt) {
+      img[q] = i0;
+      img[sp.MN + q] = al;
     }
     // calculateInu, src/functions.cu:3939-3966
     float inu = i0 * powf(nudiv, al);
@@ -200,7 +215,8 @@ __global__ void __launch_bounds__(256) k_degrid(
     const float2* __restrict__ grid, float2* __restrict__ cvr, int store,
     double* __restrict__ part, int part_stride, uint32_t* __restrict__ cmax,
     uint32_t* __restrict__ done, const int64_t* __restrict__ nvis, int normalize,
-    double* __restrict__ chi2_out) {
+    double* __restrict__ chi2_out, double* __restrict__ term_out, uint32_t zero_terms,
+    double* __restrict__ term_slots) {
   const int c = blockIdx.y;
   float mx = 0.0f;
   const ChanRange rg = ranges[c];
@@ -237,8 +253,16 @@ __global__ void __launch_bounds__(256) k_degrid(
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = acc;
-  if (last_block_done(done, gridDim.x * gridDim.y))
+  if (last_block_done(done, gridDim.x * gridDim.y)) {
     finish_chi2(gridDim.y, gridDim.x, part, part_stride, nvis, normalize, chi2_out);
+    if (threadIdx.x == 0) {
+      // ObjectiveFunction's per-term values: chi2's own slot, and 0 for the
+      // priors the iteration gating leaves out
+      if (term_out) *term_out = *chi2_out;
+      for (int t = 0; t < 32; t++)
+        if (zero_terms & (1u << t)) term_slots[t] = 0.0;
+    }
+  }
 }
 
 // ---- priors ---------------------------------------------------------------
@@ -406,7 +430,8 @@ static int cols_per_block(int n, int channels, int num_sms) {
 
 // Model grids of all channels for image d_img (clip written back when
 // write_clip).
-gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_clip) {
+gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_clip,
+                             const XtSource* xs = nullptr) {
   const int n = P.N, C = (int)P.chans.size();
   StageParams sp;
   sp.M = P.M;
@@ -429,6 +454,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.flag_opt = flag_opt;
   sp.write_clip = write_clip;
   sp.gcf = P.d_gcf;
+  sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0, 0};
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
   const size_t sm1 = sizeof(float2) * (2 * n - 1);
   if (sm1 > 48 * 1024)
@@ -446,8 +472,9 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   return GV_OK;
 }
 
-gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
-  gv_status s = model_grids_launch(P, d_img, flag_opt, 1);
+gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                      const XtSource* xs, double* term_out, uint32_t zero_terms) {
+  gv_status s = model_grids_launch(P, d_img, flag_opt, 1, xs);
   if (s != GV_OK) return s;
   const int C = (int)P.chans.size();
   int64_t maxg = 1;
@@ -462,7 +489,8 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
                                               P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride,
                                               P.d_flags + kFlagCvrMax,
                                               P.d_flags + kFlagDegridDone, P.d_chnvis,
-                                              P.normalize, P.d_scal + kSlotChi2);
+                                              P.normalize, P.d_scal + kSlotChi2, term_out,
+                                              zero_terms, P.d_scal + kSlotTerm0);
   GV_LAUNCH("k_degrid");
   return GV_OK;
 }
@@ -508,16 +536,27 @@ gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi
 }
 
 // ObjectiveFunction::calcFunction; values land in d_scal[kSlotTerm0 + t].
-gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                           const XtSource* xs) {
+  // Chi2 is the first term when present; its kernel also writes its term
+  // slot and zeroes the slots of the priors gated off
+  bool has_chi2 = false;
+  uint32_t zero = 0u;
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    if (P.terms[t].kind == GV_FI_CHI2) has_chi2 = true;
+    else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) zero |= 1u << t;
+  }
+  if (xs && !has_chi2) {
+    set_error("a line-search evaluation needs the Chi2 term");
+    return GV_ERR_UNSUPPORTED;
+  }
   for (size_t t = 0; t < P.terms.size(); t++) {
     const Term& tm = P.terms[t];
     gv_status s = GV_OK;
     if (tm.kind == GV_FI_CHI2) {
-      s = chi2_launch(P, d_img, flag_opt, store_res);
-      if (s == GV_OK) {
-        GV_CUDA(cudaMemcpyAsync(P.d_scal + kSlotTerm0 + t, P.d_scal + kSlotChi2, sizeof(double),
-                                cudaMemcpyDeviceToDevice, P.stream));
-      }
+      s = chi2_launch(P, d_img, flag_opt, store_res, xs, P.d_scal + kSlotTerm0 + t, zero);
+    } else if (has_chi2 && (zero & (1u << t))) {
+      // zeroed by the chi2 kernel
     } else if (P.iteration > 0 && tm.lambda != 0.0f) {
       s = prior_value_launch(P, (int)t, d_img, kSlotTerm0 + (int)t);
     } else {

@@ -336,8 +336,9 @@ struct Workspace {
 
 // ---- device line search: one graph launch per linmin --------------------
 // Graph: k_ls_begin, then a WHILE node whose body evaluates the objective at
-// the controller's point (k_eval_xt, the objective kernels) and advances the
-// controller (k_ls_step), which ends the loop.  One graph per set of
+// the controller's point (the objective kernels, the first of which forms
+// xt = p + x xi itself) and advances the controller (k_ls_step), which ends
+// the loop.  One graph per set of
 // buffers and objective gating, as for the evaluation graphs.
 constexpr int kLsCap = 4096;  // objective evaluations of one search at most
 
@@ -409,10 +410,9 @@ gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
     P.stream = saved;
     return cuda_fail(e, "cudaStreamBeginCaptureToGraph (line search body)");
   }
-  k_eval_xt<<<nblk(2 * MN), 256, 0, c.cap>>>(MN, 0.0f, &P.d_ls->x_req, floor_val, floor_cmp,
-                                               positivity, pcom, xicom, xt);
-  count_launch();
-  s = objective_launch(P, xt, flag, false);
+  // evaluateXt at the controller's point happens in the FFT staging kernel
+  const XtSource xs{pcom, xicom, &P.d_ls->x_req, floor_val, floor_cmp, positivity};
+  s = objective_launch(P, xt, flag, false, &xs);
   if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
   cudaGraph_t g2 = body;
   e = cudaStreamEndCapture(c.cap, &g2);
