@@ -107,6 +107,7 @@ gv_status autotune(Problem& P, gv_tune_report* rep) {
       float* np = nullptr;
       GV_CUDA(cudaMalloc(&np, sizeof(float) * (size_t)need * MN));
       GV_CUDA(cudaStreamSynchronize(P.stream));
+      graph_cache_free(P);  // captured gradients hold the old buffer
       cudaFree(P.tc_partial);
       P.tc_partial = np;
       P.tc_partial_cap = (size_t)need;
@@ -139,6 +140,7 @@ gv_status autotune(Problem& P, gv_tune_report* rep) {
   rep->candidates = ncand;
   // captured graphs hold the old launch shapes
   graph_cache_free(P);
+  ls_cache_free(P);
   return GV_OK;
 }
 

@@ -223,7 +223,8 @@ gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter, in
   GV_CHECK_PROBLEM(p);
   Problem& P = p->P;
   if (!d_img || !d_xi || iter < 0) { gv::set_error("invalid gradient arguments"); return GV_ERR_INVALID; }
-  gv_status s = gv::gradient_launch(P, d_img, d_xi, iter, flag_opt);
+  gv_status s = P.use_graphs ? gv::eval_graph(P, d_img, d_xi, iter, flag_opt, 2, false)
+                             : gv::gradient_launch(P, d_img, d_xi, iter, flag_opt);
   if (s != GV_OK) return s;
   return gv::check_device_error(P);
 }

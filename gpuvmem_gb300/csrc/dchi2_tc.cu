@@ -63,6 +63,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 #include <type_traits>
@@ -127,6 +128,9 @@ struct TcParams {
   const float* img;
   const uint32_t* cmax_bits;  // max |c| (float bits)
   const float* gcf;           // [MN] gridding correction (modes 0, 1), or null
+  const float* beam_x;        // [N] beam_coord per column / row
+  const float* beam_y;
+  const float* fac;           // [C][MN] epilogue factors (modes 0, 1; k_epi_factors)
   float* partial;             // [nsplit][MN]
   uint32_t* err;
 };
@@ -151,20 +155,21 @@ struct Layout {
   static constexpr uint32_t kSmem = 1024 + kStages * kStage + kVis + kBars + 16;
 };
 
-// Epilogue factor of one pixel for channel c (mode 0: gradient with chain
-// rule; 1: raw channel DChi2; 2: dirty image; 3: PSF; 4: the error maps'
-// sum Re(w Vr e^{+2 pi i (x u + y v)})), divided by the operand scale.
-__device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int j, float inv_s) {
-  if (p.mode >= 2) return inv_s;
+// Epilogue factor of one pixel for channel c before the operand scale
+// (mode 0: gradient with chain rule; 1: raw channel DChi2).  Modes 2 (dirty
+// image), 3 (PSF) and 4 (the error maps' sum Re(w Vr e^{+2 pi i (x u + y v)}))
+// take the operand scale alone.  The kernel multiplies by the scale 2^-e
+// afterwards: a power of two, so the product rounds as the reference's
+// order of operations does.
+__device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int j) {
   const int64_t q = (int64_t)p.N * i + j;
   if (!(p.mask[q] & kMaskIn)) return 0.0f;
   const float freq = p.chfreq[c];
-  const float atten = attenuation(i, j, p.xobs, p.yobs, p.DELTAX, p.DELTAY, freq, p.D, p.pbf,
-                                  p.pbcut, p.pb);
+  const float atten = attenuation_xy(p.beam_x[j], p.beam_y[i], freq, p.D, p.pbf, p.pbcut, p.pb);
   // fg_scale * atten (* gcf: the GCF variant, src/functions.cu:3834-3836)
   float sf = p.fg_scale * atten;
   if (p.gcf) sf *= p.gcf[q];
-  float f = -sf * inv_s;
+  float f = -sf;
   if (p.normalize) f /= (float)p.chnvis[c];
   if (p.mode == 1) return f;
   const float nudiv = freq / p.nu_0;
@@ -173,6 +178,17 @@ __device__ __forceinline__ float epi_factor(const TcParams& p, int c, int i, int
   if (p.flag_opt % 2 == 0) return f * pw;
   if (i0 > p.threshold) return f * (i0 * pw * p.fg_scale * logf(nudiv));
   return 0.0f;
+}
+
+// The factors of all pixels and channels, coalesced, before the GEMM kernel
+// (whose epilogue then reads one float per output instead of the mask, the
+// image planes, the GCF and the beam).
+__global__ void k_epi_factors(TcParams p, float* __restrict__ fac) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= p.MN) return;
+  const int c = blockIdx.y;
+  const int i = (int)(q / p.N), j = (int)(q - (int64_t)i * p.N);
+  fac[(int64_t)c * p.MN + q] = epi_factor(p, c, i, j);
 }
 
 // Two FP32 values in one 64-bit register pair, for the packed FP32x2
@@ -647,19 +663,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
           ndr++;
           run_empty = false;
           if (last) {
-            // channel epilogue: partial (+)= factor * running sum
+            // channel epilogue: partial (+)= factor * running sum; each lane
+            // owns one output row, 16-byte accesses along it
+            const float* frow =
+                p.mode <= 1 ? p.fac + (int64_t)c * p.MN + (int64_t)p.N * ei + j0 : nullptr;
 #pragma unroll 1
             for (int cb = dq * kSliceT; cb < (dq + 1) * kSliceT; cb += 32) {
               float run[32];
               tmem_ld32(t_run + lane_off + (uint32_t)cb, run);
-#pragma unroll 4
-              for (int k = 0; k < 32; k++) {
-                const float f = epi_factor(p, c, ei, j0 + cb + k, inv_s);
-                const float v = f * run[k];
-                if (first_channel)
-                  prow[cb + k] = v;
-                else
-                  prow[cb + k] += v;
+#pragma unroll
+              for (int k4 = 0; k4 < 8; k4++) {
+                float4 f = make_float4(inv_s, inv_s, inv_s, inv_s);
+                if (frow) {
+                  f = __ldg(reinterpret_cast<const float4*>(frow + cb) + k4);
+                  f = make_float4(f.x * inv_s, f.y * inv_s, f.z * inv_s, f.w * inv_s);
+                }
+                float4 v = make_float4(f.x * run[4 * k4], f.y * run[4 * k4 + 1],
+                                       f.z * run[4 * k4 + 2], f.w * run[4 * k4 + 3]);
+                float4* dst = reinterpret_cast<float4*>(prow + cb) + k4;
+                if (!first_channel) {
+                  const float4 o = *dst;
+                  v = make_float4(o.x + v.x, o.y + v.y, o.z + v.z, o.w + v.w);
+                }
+                *dst = v;
               }
             }
             first_channel = false;
@@ -754,11 +780,22 @@ __global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restric
   out[q] += (float)s;
 }
 
+// Per device and kernel variant: the shared-memory attribute is set and the
+// cluster occupancy queried once (the query costs tens of microseconds of
+// host time, which a small problem's gradient would otherwise wait for).
+constexpr int kPrepDevices = 64;
+
 template <int TN, bool PAIR, int NP>
 gv_status launch_tc(const Problem& P, const TcParams& p, int nitems) {
   auto kern = k_dchi2_tc<TN, PAIR, NP>;
   const size_t smem = Layout<TN, PAIR, NP>::kSmem;
-  GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static std::atomic<int> prepared[kPrepDevices];  // 0: not yet; else active clusters + 1
+  int dev = 0;
+  GV_CUDA(cudaGetDevice(&dev));
+  const bool cacheable = dev >= 0 && dev < kPrepDevices;
+  int known = cacheable ? prepared[dev].load(std::memory_order_acquire) : 0;
+  if (known == 0)
+    GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   cfg.blockDim = dim3(kThreads, 1, 1);
@@ -774,13 +811,18 @@ gv_status launch_tc(const Problem& P, const TcParams& p, int nitems) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3(2 * nclusters, 1, 1);
-    int active = 0;
-    GV_CUDA(cudaOccupancyMaxActiveClusters(&active, kern, &cfg));
+    int active = known - 1;
+    if (known == 0) {
+      GV_CUDA(cudaOccupancyMaxActiveClusters(&active, kern, &cfg));
+      if (cacheable && active > 0) prepared[dev].store(active + 1, std::memory_order_release);
+    }
     if (active <= 0) {
       set_error("no CTA pair of the tensor-core DChi2 kernel fits on this device");
       return GV_ERR_UNSUPPORTED;
     }
     nclusters = std::min(nclusters, active);
+  } else if (cacheable && known == 0) {
+    prepared[dev].store(1, std::memory_order_release);
   }
   nclusters = std::max(1, std::min(nclusters, nitems));
   cfg.gridDim = dim3(cs * nclusters, 1, 1);
@@ -866,6 +908,23 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
     p.C = (int)P.chans.size();
     p.kc_off = P.d_kc_off;
     p.Ktot = P.Vgrid;
+  }
+  p.beam_x = P.d_beam_x;
+  p.beam_y = P.d_beam_y;
+  p.fac = nullptr;
+  if (mode <= 1) {
+    const size_t need = sizeof(float) * (size_t)p.C * (size_t)p.MN;
+    if (P.epi_bytes < need) {
+      cudaFree(P.d_epi);
+      P.d_epi = nullptr;
+      P.epi_bytes = 0;
+      GV_CUDA(cudaMalloc(&P.d_epi, need));
+      P.epi_bytes = need;
+    }
+    p.fac = P.d_epi;
+    tc::k_epi_factors<<<dim3((unsigned)((p.MN + 255) / 256), (unsigned)p.C), 256, 0, P.stream>>>(
+        p, P.d_epi);
+    GV_LAUNCH("k_epi_factors");
   }
   const int nitems = (p.ntile_i / (pair ? 2 : 1)) * p.ntile_j * p.nsplit;
   // accumulator parts: 2 lets the first half drain while the tensor core

@@ -52,13 +52,13 @@ void graph_cache_free(Problem& P) {
   P.graphs = nullptr;
 }
 
-// what: 1 = objective, 3 = objective + gradient; store: the objective
-// keeps its weighted residuals for the next gradient.  The objective's
+// what: 1 = objective, 2 = gradient, 3 = objective + gradient; store: the
+// objective keeps its weighted residuals for the next gradient.  The objective's
 // scalars land in d_scal as with objective_launch; the caller fetches them.
 gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt, int what,
                      bool store) {
   GraphCache& c = cache(P);
-  const int obj_gate = P.iteration > 0 ? 1 : 0;
+  const int obj_gate = (what & 1) ? (P.iteration > 0 ? 1 : 0) : 0;
   const int grad_gate = (what & 2) ? (iter > 0 ? 1 : 0) : 0;
   const float* xi_key = (what & 2) ? d_xi : nullptr;
   GraphEntry* hit = nullptr;
@@ -77,7 +77,7 @@ gv_status eval_graph(Problem& P, float* d_img, float* d_xi, int iter, int flag_o
       P.stream = saved;
       return cuda_fail(e, "cudaStreamBeginCapture");
     }
-    gv_status s = objective_launch(P, d_img, flag_opt, store);
+    gv_status s = (what & 1) ? objective_launch(P, d_img, flag_opt, store) : GV_OK;
     if (s == GV_OK && (what & 2)) s = gradient_launch(P, d_img, d_xi, iter, flag_opt);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(c.cap, &graph);

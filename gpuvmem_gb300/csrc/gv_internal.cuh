@@ -43,7 +43,7 @@ enum FlagSlot {
   kFlagErr = 2,       // non-zero: a kernel gave up on a bounded wait
   kFlagPsfMax = 3,    // max weight of a kept visibility (float bits)
   kFlagDegridDone = 4,  // blocks of k_degrid done (the last one finishes chi2)
-  kFlagPriorDone = 5,   // blocks of k_prior_value done (the last one sums)
+  kFlagPriorDone = 5,   // blocks of k_prior_values done (the last one sums)
   kFlagOptDone = 6,     // blocks of an optimiser reduction done (the last one sums)
   kNumFlags = 8
 };
@@ -111,6 +111,10 @@ struct Problem {
   float* d_rho = nullptr;        // [MN] z - 1 + r^2/2 per pixel
   float2* d_grid = nullptr;      // [C][MN] model grids
   float2* d_twiddle = nullptr;   // [n-1] e^{+2 pi i k/n}, stage-major (objective.cu smem_fft)
+  float* d_beam_x = nullptr;     // [N] beam_coord of each column (attenuation)
+  float* d_beam_y = nullptr;     // [M] beam_coord of each row
+  float* d_rot_u = nullptr;      // [N] phase_rotate's u of each column (k_cols_fft)
+  float* d_rot_v = nullptr;      // [M] phase_rotate's v of each row
   double* d_part = nullptr;      // reduction partials
   int part_stride = 0;           // partials per channel / term
   double* d_scal = nullptr;      // [kNumScal]
@@ -136,6 +140,8 @@ struct Problem {
   int use_graphs = 1;            // optimizer evaluations replayed from CUDA graphs
   int tc_pair_mode = -1;         // -1: GV_TC_PAIR / default, 0 single CTAs, 1 CTA pairs
   size_t tc_partial_cap = 0;     // split-K partial images the buffer holds
+  float* d_epi = nullptr;        // [C][MN] DChi2 epilogue factors (allocated on first use)
+  size_t epi_bytes = 0;
   int degrid_threads = 256;      // k_degrid block size
   int degrid_blocks = 0;         // k_degrid blocks per channel cap (0: part_stride)
   void* graphs = nullptr;        // graph cache (graph.cu)
@@ -178,14 +184,19 @@ void add_launches(int64_t n);
 // freq_to_wavelength, src/MSFITSIO.cu:36-39 (float)
 __host__ __device__ inline float wavelength(float freq) { return kLightSpeed / freq; }
 
+// Sky offset of pixel index k from the beam centre k0 in radians, as the
+// reference's attenuation() forms it (FP64 product, rounded to float).
+// Problem::d_beam_x / d_beam_y hold it per column / row, so the hot kernels
+// do no FP64 arithmetic for it.
+__host__ __device__ inline float beam_coord(int k, int k0, double delta) {
+  return (float)((k - k0) * delta * kRpDegD);
+}
+
 // attenuation(), src/functions.cu:2304-2333, with the Gaussian and Airy
-// beams of :2275-2302; float arithmetic as the reference.
-__device__ inline float attenuation(int i, int j, float xobs, float yobs,
-                                    double DELTAX, double DELTAY, float freq,
-                                    float D, float pbf, float cutoff, int pb) {
-  const int x0 = (int)xobs, y0 = (int)yobs;
-  const float x = (float)((j - x0) * DELTAX * kRpDegD);
-  const float y = (float)((i - y0) * DELTAY * kRpDegD);
+// beams of :2275-2302; float arithmetic as the reference, from the pixel's
+// offsets x, y (beam_coord).
+__device__ inline float attenuation_xy(float x, float y, float freq, float D, float pbf,
+                                       float cutoff, int pb) {
   const float arc = sqrtf(x * x + y * y);
   const float lambda = wavelength(freq);
   float atten;
@@ -203,6 +214,13 @@ __device__ inline float attenuation(int i, int j, float xobs, float yobs,
     }
   }
   return arc <= cutoff ? atten : 0.0f;
+}
+
+__device__ inline float attenuation(int i, int j, float xobs, float yobs,
+                                    double DELTAX, double DELTAY, float freq,
+                                    float D, float pbf, float cutoff, int pb) {
+  return attenuation_xy(beam_coord(j, (int)xobs, DELTAX), beam_coord(i, (int)yobs, DELTAY), freq,
+                        D, pbf, cutoff, pb);
 }
 
 // True in every thread of the block that finishes last of `nblocks` (after
@@ -254,6 +272,7 @@ void free_problem(Problem& P);
 // A line-search point as the objective's input: xt = pcom + (*x_dev) xicom,
 // plane 0 floored at floor_val (positivity), evaluateXt of
 // src/functions.cu:2832-2864, formed inside the FFT staging (which writes xt)
+// and, per pixel, inside the prior kernel of the line search
 struct XtSource {
   const float* pcom;
   const float* xicom;
@@ -267,8 +286,9 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
                       uint32_t zero_terms = 0u);
 gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot);
 gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi);
-gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
-                           const XtSource* xs = nullptr);
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
+                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 gv_status fetch_scalars(Problem& P, int n);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);

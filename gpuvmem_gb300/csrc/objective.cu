@@ -60,6 +60,30 @@ __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restr
   }
 }
 
+// evaluateXt at one pixel (k_eval_xt's arithmetic): xt = pcom + x xicom,
+// plane 0 floored when positivity is on, plane 1 free.
+__device__ __forceinline__ void xt_pixel(const XtSource& xs, float x, int64_t MN, int64_t q,
+                                         float& i0, float& al) {
+  const float v0 = fmaf(x, xs.xicom[q], xs.pcom[q]);
+  i0 = (xs.positivity && !((double)v0 > xs.floor_cmp)) ? xs.floor_val : v0;
+  al = fmaf(x, xs.xicom[MN + q], xs.pcom[MN + q]);
+}
+
+// What clip2IWNoise (src/functions.cu:2694-2719) leaves at one pixel.
+struct ClipRule {
+  float clip_i0, threshold;
+  int flag_opt;
+};
+
+__device__ __forceinline__ void clip_pixel(uint8_t m, const ClipRule& cr, float& i0, float& al) {
+  if (m & kMaskClip) {
+    i0 = cr.clip_i0;
+    al = 0.0f;
+  } else if (i0 < cr.threshold && cr.flag_opt > 0) {
+    al = 0.0f;
+  }
+}
+
 struct StageParams {
   int M, N, log2n;
   int64_t MN;
@@ -70,6 +94,8 @@ struct StageParams {
   int flag_opt;
   int write_clip;
   const float* gcf;  // gridding correction, or null
+  const float* beam_x;  // beam_coord per column / row
+  const float* beam_y;
   XtSource xs;       // xs.pcom set: the image is xt = pcom + x xicom (written back)
 };
 
@@ -87,45 +113,37 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
   const float freq = chfreq[c];
   const float nudiv = freq / sp.nu_0;
   const float floor_inu = -1.0f * sp.eta * sp.minpix;
-  const float clip_i0 = sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix);
+  const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
+                    sp.flag_opt};
   const bool writer = sp.write_clip && c == 0;
   const bool from_xt = sp.xs.pcom != nullptr;
   const float x = from_xt ? *sp.xs.x_dev : 0.0f;
+  const float by = __ldg(sp.beam_y + i);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const int64_t q = (int64_t)n * i + j;
     float i0, al;
     if (from_xt) {
-      // evaluateXt (k_eval_xt's arithmetic): plane 0 floored, plane 1 free
-      const float v0 = fmaf(x, sp.xs.xicom[q], sp.xs.pcom[q]);
-      i0 = (sp.xs.positivity && !((double)v0 > sp.xs.floor_cmp)) ? sp.xs.floor_val : v0;
-      al = fmaf(x, sp.xs.xicom[sp.MN + q], sp.xs.pcom[sp.MN + q]);
+      xt_pixel(sp.xs, x, sp.MN, q, i0, al);
     } else {
       i0 = img[q];
       al = img[sp.MN + q];
     }
-    const uint8_t m = mask[q];
-    // clip2IWNoise, src/functions.cu:2694-2719 (mutates the image)
-    if (m & kMaskClip) {
-      if (writer && !from_xt && (i0 != clip_i0 || al != 0.0f)) {
-        img[q] = clip_i0;
-        img[sp.MN + q] = 0.0f;
-      }
-      i0 = clip_i0;
-      al = 0.0f;
-    } else if (i0 < sp.threshold && sp.flag_opt > 0) {
-      if (writer && !from_xt && al != 0.0f) img[sp.MN + q] = 0.0f;
-      al = 0.0f;
-    }
+    // clip2IWNoise, src/functions.cu:2694-2719 (mutates the image: only the
+    // pixels it changes are written back)
+    const float i0_in = i0, al_in = al;
+    clip_pixel(mask[q], cr, i0, al);
     if (writer && from_xt) {
       img[q] = i0;
       img[sp.MN + q] = al;
+    } else if (writer) {
+      if (i0 != i0_in) img[q] = i0;
+      if (al != al_in) img[sp.MN + q] = al;
     }
     // calculateInu, src/functions.cu:3939-3966
     float inu = i0 * powf(nudiv, al);
     if (inu < floor_inu) inu = floor_inu;
     // apply_beam2I, src/functions.cu:2424-2444
-    const float a = attenuation(i, j, sp.xobs, sp.yobs, sp.DELTAX, sp.DELTAY, freq, sp.D,
-                                sp.pbf, sp.pbcut, sp.pb);
+    const float a = attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
     float v = inu * a * sp.fg_scale;
     if (sp.gcf) v *= sp.gcf[q];  // apply_GCF, src/functions.cu:2468
     buf[bitrev(j, sp.log2n)] = make_float2(v, 0.0f);
@@ -138,8 +156,9 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
 
 // Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate
 // (src/functions.cu:2483-2518) in the reference's float arithmetic.
-__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, float xphs, float yphs,
-                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
+__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __restrict__ rot_u,
+                           const float* __restrict__ rot_v, const float2* __restrict__ tw_g,
+                           float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
   const int n = N;
   float2* buf = sm;
@@ -153,13 +172,13 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, float xphs, flo
   }
   __syncthreads();
   smem_fft(buf, log2n, cb, tw);
-  const double upix = (double)xphs / (double)n;
-  const double vpix = (double)yphs / (double)n;
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
     const int j = j0 + cc;
-    const float u = (float)(j < n / 2 ? upix * j : upix * (j - n));
-    const float v = (float)(r < n / 2 ? vpix * r : vpix * (r - n));
+    // u = xphs / n * (j or j - n), v likewise for the row, in FP64 rounded
+    // to float (the tables hold them)
+    const float u = __ldg(rot_u + j);
+    const float v = __ldg(rot_v + r);
     const float phase = -2.0f * (u + v);
     float s, co;
     sincospif(phase, &s, &co);
@@ -278,8 +297,8 @@ struct PriorParams {
 // Value of one pixel, src/functions.cu:2882 (L1), 3036 (S), 3238 (TV),
 // 3353 (TSV), 3443 (L), 3114 (SGVector), 2954 (GL1), 3141 (QP); the caller
 // has checked the mask.
-__device__ __forceinline__ float prior_pixel(const PriorParams& pp, const float* __restrict__ I,
-                                             int i, int j) {
+template <class Img>
+__device__ __forceinline__ float prior_pixel(const PriorParams& pp, const Img& I, int i, int j) {
   const int N = pp.N;
   const float c = I[(int64_t)N * i + j];
   switch (pp.kind) {
@@ -379,12 +398,52 @@ __device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
   return 0.0f;
 }
 
-// prior value partials; the last block to finish sums them in a fixed order
-__global__ void __launch_bounds__(256) k_prior_value(PriorParams pp, const float* __restrict__ I,
-                                                     const uint8_t* __restrict__ mask,
-                                                     double* __restrict__ part,
-                                                     uint32_t* __restrict__ done,
-                                                     double* __restrict__ out) {
+// Images the prior values read.  PlainImage: an image in memory.  XtImage:
+// the line search's xt = pcom + x xicom, formed per pixel with the FFT
+// staging's arithmetic and clipped as clip2IWNoise leaves it (Chi2, the
+// first term, clips the image the priors then see), so the priors need not
+// wait for the staging kernel to write xt.
+struct PlainImage {
+  const float* p;
+  __device__ void bind() {}
+  __device__ __forceinline__ float operator[](int64_t q) const { return p[q]; }
+};
+
+struct XtImage {
+  XtSource xs;
+  const uint8_t* mask;
+  int64_t MN;
+  ClipRule cr;
+  int plane;
+  float x;
+  __device__ void bind() { x = *xs.x_dev; }
+  __device__ __forceinline__ float operator[](int64_t q) const {
+    float i0, al;
+    xt_pixel(xs, x, MN, q, i0, al);
+    clip_pixel(mask[q], cr, i0, al);
+    return plane ? al : i0;
+  }
+};
+
+template <class Img>
+struct PriorSet {
+  int n;
+  PriorParams pp[kMaxTerms];
+  Img img[kMaxTerms];
+  double* part[kMaxTerms];  // gridDim.x partial sums per term
+  double* out[kMaxTerms];   // the term's value
+};
+
+// Values of n prior terms (blockIdx.y = term): per-block partials, and the
+// last block to finish sums each term's partials in a fixed order.
+template <class Img>
+__global__ void __launch_bounds__(256) k_prior_values(PriorSet<Img> ps,
+                                                      const uint8_t* __restrict__ mask,
+                                                      uint32_t* __restrict__ done) {
+  const int t = blockIdx.y;
+  const PriorParams pp = ps.pp[t];
+  Img I = ps.img[t];
+  I.bind();
   double acc = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
        q += (int64_t)gridDim.x * blockDim.x) {
@@ -393,12 +452,14 @@ __global__ void __launch_bounds__(256) k_prior_value(PriorParams pp, const float
     acc += (double)prior_pixel(pp, I, i, j);
   }
   acc = block_sum(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
-  if (last_block_done(done, gridDim.x)) {
-    double v = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(part + b);
-    v = block_sum(v);
-    if (threadIdx.x == 0) *out = v;
+  if (threadIdx.x == 0) ps.part[t][blockIdx.x] = acc;
+  if (last_block_done(done, gridDim.x * gridDim.y)) {
+    for (int u = 0; u < ps.n; u++) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(ps.part[u] + b);
+      v = block_sum(v);
+      if (threadIdx.x == 0) *ps.out[u] = v;
+    }
   }
 }
 
@@ -454,6 +515,8 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.flag_opt = flag_opt;
   sp.write_clip = write_clip;
   sp.gcf = P.d_gcf;
+  sp.beam_x = P.d_beam_x;
+  sp.beam_y = P.d_beam_y;
   sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0, 0};
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
   const size_t sm1 = sizeof(float2) * (2 * n - 1);
@@ -466,8 +529,8 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n - 1);
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-  k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.xobs, P.yobs,
-                                                      P.d_twiddle, P.d_grid);
+  k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
+                                                      P.d_rot_v, P.d_twiddle, P.d_grid);
   GV_LAUNCH("k_cols_fft");
   return GV_OK;
 }
@@ -509,16 +572,41 @@ static PriorParams prior_params(const Problem& P, const Term& t) {
   return pp;
 }
 
-gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot) {
-  const Term& tm = P.terms[t];
-  PriorParams pp = prior_params(P, tm);
-  const int64_t MN = pp.MN;
-  int nb = (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
-  double* part = P.d_part + (int64_t)P.part_stride * (P.chans.size() + t);
-  k_prior_value<<<nb, 256, 0, P.stream>>>(pp, d_img + MN * tm.image_index, P.d_mask, part,
-                                          P.d_flags + kFlagPriorDone, P.d_scal + slot);
-  GV_LAUNCH("k_prior_value");
+static int prior_blocks(const Problem& P) {
+  const int64_t MN = (int64_t)P.M * P.N;
+  return (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
+}
+
+static double* prior_part(Problem& P, int t) {
+  return P.d_part + (int64_t)P.part_stride * (P.chans.size() + t);
+}
+
+template <class Img>
+static gv_status prior_values_launch(Problem& P, cudaStream_t st, const PriorSet<Img>& ps) {
+  k_prior_values<Img><<<dim3(prior_blocks(P), ps.n), 256, 0, st>>>(ps, P.d_mask,
+                                                                    P.d_flags + kFlagPriorDone);
+  GV_LAUNCH("k_prior_values");
   return GV_OK;
+}
+
+// Values of the terms ts[0..n) of image d_img, into d_scal[slot[k]].
+static gv_status prior_values_plain(Problem& P, const int* ts, const int* slots, int n,
+                                    const float* d_img) {
+  PriorSet<PlainImage> ps{};
+  ps.n = n;
+  const int64_t MN = (int64_t)P.M * P.N;
+  for (int k = 0; k < n; k++) {
+    const Term& tm = P.terms[ts[k]];
+    ps.pp[k] = prior_params(P, tm);
+    ps.img[k] = PlainImage{d_img + MN * tm.image_index};
+    ps.part[k] = prior_part(P, ts[k]);
+    ps.out[k] = P.d_scal + slots[k];
+  }
+  return prior_values_launch(P, P.stream, ps);
+}
+
+gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot) {
+  return prior_values_plain(P, &t, &slot, 1, d_img);
 }
 
 gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi) {
@@ -536,34 +624,87 @@ gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi
 }
 
 // ObjectiveFunction::calcFunction; values land in d_scal[kSlotTerm0 + t].
-gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
-                           const XtSource* xs) {
-  // Chi2 is the first term when present; its kernel also writes its term
-  // slot and zeroes the slots of the priors gated off
+// Terms are evaluated in list order; consecutive active priors share one
+// launch.
+gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res) {
+  // Chi2 also writes its term slot and zeroes the slots of the priors the
+  // iteration gating leaves out
   bool has_chi2 = false;
   uint32_t zero = 0u;
   for (size_t t = 0; t < P.terms.size(); t++) {
     if (P.terms[t].kind == GV_FI_CHI2) has_chi2 = true;
     else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) zero |= 1u << t;
   }
-  if (xs && !has_chi2) {
-    set_error("a line-search evaluation needs the Chi2 term");
-    return GV_ERR_UNSUPPORTED;
-  }
+  int run[kMaxTerms], slots[kMaxTerms], nrun = 0;
+  auto flush = [&]() -> gv_status {
+    const int n = nrun;
+    nrun = 0;
+    return n ? prior_values_plain(P, run, slots, n, d_img) : GV_OK;
+  };
   for (size_t t = 0; t < P.terms.size(); t++) {
     const Term& tm = P.terms[t];
     gv_status s = GV_OK;
     if (tm.kind == GV_FI_CHI2) {
-      s = chi2_launch(P, d_img, flag_opt, store_res, xs, P.d_scal + kSlotTerm0 + t, zero);
+      s = flush();
+      if (s == GV_OK) s = chi2_launch(P, d_img, flag_opt, store_res, nullptr, P.d_scal + kSlotTerm0 + t, zero);
     } else if (has_chi2 && (zero & (1u << t))) {
       // zeroed by the chi2 kernel
     } else if (P.iteration > 0 && tm.lambda != 0.0f) {
-      s = prior_value_launch(P, (int)t, d_img, kSlotTerm0 + (int)t);
+      if (nrun == kMaxTerms) s = flush();
+      run[nrun] = (int)t;
+      slots[nrun] = kSlotTerm0 + (int)t;
+      nrun++;
     } else {
       GV_CUDA(cudaMemsetAsync(P.d_scal + kSlotTerm0 + t, 0, sizeof(double), P.stream));
     }
     if (s != GV_OK) return s;
   }
+  return flush();
+}
+
+// One objective evaluation of the line search at the controller's point:
+// the Chi2 kernels on P.stream (the staging kernel forms xt and writes it
+// to d_xt), the active priors in one launch on `side`, forked from P.stream
+// through `fork` and joined back through `join`; the priors form xt
+// themselves, so both branches run at once.
+gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
+                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+  int ichi2 = -1;
+  uint32_t zero = 0u;
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    if (P.terms[t].kind == GV_FI_CHI2) {
+      if (ichi2 < 0) ichi2 = (int)t;
+    } else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) {
+      zero |= 1u << t;
+    }
+  }
+  if (ichi2 < 0) {
+    set_error("a line-search evaluation needs the Chi2 term");
+    return GV_ERR_UNSUPPORTED;
+  }
+  PriorSet<XtImage> ps{};
+  const int64_t MN = (int64_t)P.M * P.N;
+  const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
+                    flag_opt};
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    const Term& tm = P.terms[t];
+    if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
+    const int k = ps.n++;
+    ps.pp[k] = prior_params(P, tm);
+    ps.img[k] = XtImage{xs, P.d_mask, MN, cr, tm.image_index, 0.0f};
+    ps.part[k] = prior_part(P, (int)t);
+    ps.out[k] = P.d_scal + kSlotTerm0 + t;
+  }
+  if (ps.n > 0) {
+    GV_CUDA(cudaEventRecord(fork, P.stream));
+    GV_CUDA(cudaStreamWaitEvent(side, fork, 0));
+    gv_status s = prior_values_launch(P, side, ps);
+    if (s != GV_OK) return s;
+    GV_CUDA(cudaEventRecord(join, side));
+  }
+  gv_status s = chi2_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero);
+  if (s != GV_OK) return s;
+  if (ps.n > 0) GV_CUDA(cudaStreamWaitEvent(P.stream, join, 0));
   return GV_OK;
 }
 

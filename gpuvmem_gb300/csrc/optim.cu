@@ -336,10 +336,11 @@ struct Workspace {
 
 // ---- device line search: one graph launch per linmin --------------------
 // Graph: k_ls_begin, then a WHILE node whose body evaluates the objective at
-// the controller's point (the objective kernels, the first of which forms
-// xt = p + x xi itself) and advances the controller (k_ls_step), which ends
-// the loop.  One graph per set of
-// buffers and objective gating, as for the evaluation graphs.
+// the controller's point and advances the controller (k_ls_step), which ends
+// the loop.  The body has two branches: the Chi2 kernels (the first forms
+// xt = p + x xi itself and writes it) and one kernel for the active priors
+// (which forms xt per pixel too); k_ls_step waits for both.  One graph per
+// set of buffers and objective gating, as for the evaluation graphs.
 constexpr int kLsCap = 4096;  // objective evaluations of one search at most
 
 struct LsEntry {
@@ -353,7 +354,9 @@ struct LsEntry {
 };
 struct LsCache {
   std::vector<LsEntry> e;
-  cudaStream_t cap = nullptr;
+  cudaStream_t cap = nullptr;   // capture stream (the evaluation's main branch)
+  cudaStream_t side = nullptr;  // the priors' branch
+  cudaEvent_t fork = nullptr, join = nullptr;
   uint64_t clock = 0;
 };
 constexpr size_t kMaxLsGraphs = 4;
@@ -368,6 +371,9 @@ gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
                          double floor_cmp, const LsTerms& terms, cudaGraphExec_t* out,
                          int64_t* body_launches) {
   if (!c.cap) GV_CUDA(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
+  if (!c.side) GV_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+  if (!c.fork) GV_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+  if (!c.join) GV_CUDA(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
   cudaGraph_t root = nullptr;
   GV_CUDA(cudaGraphCreate(&root, 0));
   struct Guard {
@@ -411,8 +417,9 @@ gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
     return cuda_fail(e, "cudaStreamBeginCaptureToGraph (line search body)");
   }
   // evaluateXt at the controller's point happens in the FFT staging kernel
+  // (and in the prior kernel, which runs beside the Chi2 kernels)
   const XtSource xs{pcom, xicom, &P.d_ls->x_req, floor_val, floor_cmp, positivity};
-  s = objective_launch(P, xt, flag, false, &xs);
+  s = ls_objective_launch(P, xt, flag, xs, c.side, c.fork, c.join);
   if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
   cudaGraph_t g2 = body;
   e = cudaStreamEndCapture(c.cap, &g2);
@@ -432,6 +439,9 @@ void ls_cache_free(Problem& P) {
   LsCache* c = static_cast<LsCache*>(P.ls_graphs);
   for (auto& g : c->e) cudaGraphExecDestroy(g.exec);
   if (c->cap) cudaStreamDestroy(c->cap);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->fork) cudaEventDestroy(c->fork);
+  if (c->join) cudaEventDestroy(c->join);
   delete c;
   P.ls_graphs = nullptr;
 }
@@ -515,7 +525,8 @@ class Solver {
 
   gv_status grad(float* img, float* xi, int iter) {
     n_grad_++;
-    return gradient_launch(P_, img, xi, iter, o_.flag);
+    return P_.use_graphs ? eval_graph(P_, img, xi, iter, o_.flag, 2, false)
+                         : gradient_launch(P_, img, xi, iter, o_.flag);
   }
 
   // f1dim: xt = pcom + x*xicom (floored on plane 0), then the objective.

@@ -182,6 +182,8 @@ void free_problem(Problem& P) {
   cudaFree(P.d_rho);
   cudaFree(P.d_grid);
   cudaFree(P.d_twiddle);
+  cudaFree(P.d_beam_x);  // one allocation with d_beam_y, d_rot_u, d_rot_v
+  cudaFree(P.d_epi);
   cudaFree(P.d_part);
   cudaFree(P.d_scal);
   cudaFree(P.d_tmp);
@@ -516,6 +518,29 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * (n - 1),
                             cudaMemcpyHostToDevice, st));
   }
+  {
+    // per-column / per-row FP64 products of attenuation() and phase_rotate
+    // (src/functions.cu:2304-2310, :2490-2500), rounded to float once here
+    // (IEEE products: the same floats the kernels would form)
+    std::vector<float> bx(P.N), by(P.M), ru(P.N), rv(P.M);
+    const double upix = (double)P.xobs / (double)P.N, vpix = (double)P.yobs / (double)P.M;
+    for (int j = 0; j < P.N; j++) {
+      bx[j] = beam_coord(j, (int)P.xobs, P.DELTAX);
+      ru[j] = (float)(j < P.N / 2 ? upix * j : upix * (j - P.N));
+    }
+    for (int i = 0; i < P.M; i++) {
+      by[i] = beam_coord(i, (int)P.yobs, P.DELTAY);
+      rv[i] = (float)(i < P.M / 2 ? vpix * i : vpix * (i - P.M));
+    }
+    GV_CUDA(cudaMalloc(&P.d_beam_x, sizeof(float) * 2 * (P.N + P.M)));
+    P.d_beam_y = P.d_beam_x + P.N;
+    P.d_rot_u = P.d_beam_y + P.M;
+    P.d_rot_v = P.d_rot_u + P.N;
+    GV_CUDA(cudaMemcpy(P.d_beam_x, bx.data(), sizeof(float) * P.N, cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_beam_y, by.data(), sizeof(float) * P.M, cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_rot_u, ru.data(), sizeof(float) * P.N, cudaMemcpyHostToDevice));
+    GV_CUDA(cudaMemcpy(P.d_rot_v, rv.data(), sizeof(float) * P.M, cudaMemcpyHostToDevice));
+  }
   GV_CUDA(cudaMalloc(&P.d_grid, sizeof(float2) * MN * C));
   {
     std::vector<float> f(C);
@@ -575,6 +600,9 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     P.tc_fast_anchor = (acc && acc[0] == '1') ? 0 : 1;
     GV_CUDA(cudaMalloc(&P.tc_partial, sizeof(float) * (size_t)best * MN));
     P.tc_partial_cap = (size_t)best;
+    // epilogue factors of every channel (set up here, not inside a capture)
+    P.epi_bytes = sizeof(float) * (size_t)C * (size_t)MN;
+    GV_CUDA(cudaMalloc(&P.d_epi, P.epi_bytes));
   }
   {
     const char* g = std::getenv("GV_GRAPHS");

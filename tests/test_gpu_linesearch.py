@@ -14,15 +14,15 @@ from gpuvmem_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _solve(device_ls, method, iterations, seed, n=64, nchan=1, device_lbfgs=True):
+def _solve(device_ls, method, iterations, seed, n=64, nchan=1, device_lbfgs=True, terms=None):
     import torch
     import gpuvmem_gb300 as gv
     os.environ["GV_DEVICE_LS"] = "1" if device_ls else "0"
     os.environ["GV_DEVICE_LBFGS"] = "1" if device_lbfgs else "0"
     try:
         data = synth.generate(synth.small_config(n=n, nchan=nchan, seed=seed), device="cuda")
-        prob = gv.Problem(data, [gv.term("Chi2", 1.0), gv.term("Entropy", 0.01),
-                                 gv.term("TotalSquaredVariation", 1e-5)])
+        terms = terms or [("Chi2", 1.0), ("Entropy", 0.01), ("TotalSquaredVariation", 1e-5)]
+        prob = gv.Problem(data, [gv.term(k, lam) for k, lam in terms])
         img = prob.initial_image()
         rep = prob.optimize(img, method, iterations=iterations)
         torch.cuda.synchronize()
@@ -46,6 +46,17 @@ def test_device_line_search_two_channels_128():
     rh, ih = _solve(False, "CG-FRPRMN", 8, seed=5, n=128, nchan=2)
     rd, idv = _solve(True, "CG-FRPRMN", 8, seed=5, n=128, nchan=2)
     assert rd.n_objective == rh.n_objective
+    np.testing.assert_array_equal(idv.view(np.uint32), ih.view(np.uint32))
+
+
+def test_device_line_search_three_priors():
+    """Three priors in one prior kernel that forms xt itself (clip2IWNoise
+    applied, as Chi2 comes first) and runs beside the Chi2 kernels."""
+    terms = [("Chi2", 1.0), ("Entropy", 0.01), ("TotalSquaredVariation", 1e-5), ("L1-Norm", 1e-4)]
+    rh, ih = _solve(False, "CG-FRPRMN", 10, seed=9, terms=terms)
+    rd, idv = _solve(True, "CG-FRPRMN", 10, seed=9, terms=terms)
+    assert rd.iterations == rh.iterations and rd.n_objective == rh.n_objective
+    assert np.float32(rd.f_final).tobytes() == np.float32(rh.f_final).tobytes()
     np.testing.assert_array_equal(idv.view(np.uint32), ih.view(np.uint32))
 
 
