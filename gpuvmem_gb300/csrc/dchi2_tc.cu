@@ -52,7 +52,7 @@
 //                       in the peer CTA, lane 0 forwards the stage's
 //                       completion to the leader (one cluster-scope arrive
 //                       per chunk instead of one per generator warp).
-// Split-K partials are summed in FP64 in a fixed order, so results are
+// Split-K partials are summed (compensated, FP64-grade) in a fixed order, so results are
 // deterministic.
 //
 // Every wait is bounded: on timeout the kernel records an error word, every
@@ -770,14 +770,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_dchi2_tc(TcParams p) {
   if (warp == 0) tmem_dealloc<PAIR>(tbase, kTmemCols);
 }
 
-// result[plane][q] += sum_s partial[s][q] (FP64, fixed order)
+// result[plane][q] += sum_s partial[s][q] (compensated, fixed order)
 __global__ void k_reduce_partials(int64_t MN, int nsplit, const float* __restrict__ partial,
                                   float* __restrict__ out) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= MN) return;
-  double s = 0.0;
-  for (int k = 0; k < nsplit; k++) s += (double)partial[(int64_t)k * MN + q];
-  out[q] += (float)s;
+  CompSum s;
+  for (int k = 0; k < nsplit; k++) s.add(partial[(int64_t)k * MN + q]);
+  out[q] += (float)s.value();
 }
 
 // Per device and kernel variant: the shared-memory attribute is set and the

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -223,6 +224,31 @@ __device__ inline float attenuation(int i, int j, float xobs, float yobs,
                         D, pbf, cutoff, pb);
 }
 
+// A thread's running sum of FP32 terms in FP32 instructions with Neumaier's
+// compensation (Neumaier 1974): s + c carries the sum to about 2^-48
+// relative for the few hundred terms a thread adds, as an FP64 accumulator
+// would, without the FP64 pipe (a small fraction of the FP32 rate on this
+// GPU).  value() hands the pair to the FP64 block and grid reductions.
+struct CompSum {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    c = __fadd_rn(c, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x)
+                                           : __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// The largest float not above d: for a float v, (double)v > d exactly when
+// v > float_below(d), so a comparison the reference makes in FP64 runs in
+// FP32 with the same outcome.
+inline float float_below(double d) {
+  float f = (float)d;
+  if ((double)f > d) f = std::nextafter(f, -HUGE_VALF);
+  return f;
+}
+
 // True in every thread of the block that finishes last of `nblocks` (after
 // each block stored its partials); that block resets the counter for the
 // next launch.  It then combines the partials in a fixed order, so the
@@ -278,7 +304,7 @@ struct XtSource {
   const float* xicom;
   const float* x_dev;
   float floor_val;
-  double floor_cmp;
+  float floor_cmp;  // float_below(-eta * minpix): v > floor_cmp as in FP64
   int positivity;
 };
 gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,

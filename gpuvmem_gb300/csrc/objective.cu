@@ -32,11 +32,22 @@ __device__ __forceinline__ unsigned bitrev(unsigned x, int bits) {
   return __brev(x) >> (32 - bits);
 }
 
+// Shared-memory position of element e of a length-2^log2n column: the low
+// 4 bits are XORed with 4 higher bits, so the bit-reversed scatter (lanes
+// 2^(log2n-5) elements apart, all in one bank pair unswizzled) spreads over
+// all 16 eight-byte slots of a 128-byte row, while runs of consecutive
+// elements stay conflict-free.  A bijection on [0, 2^log2n).
+__device__ __forceinline__ int swz(int e, int log2n) {
+  const int sh = log2n >= 8 ? log2n - 4 : 4;
+  return e ^ ((e >> sh) & 15);
+}
+
 // In-place inverse radix-2 DIT FFT of `ncol` independent columns of length
-// n = 2^log2n held in shared memory (column c at buf + c*n), input in
-// bit-reversed order, output in natural order.  tw is the stage-major
-// twiddle table (stage s at offset 2^(s-1) - 1), so the lanes of a warp read
-// consecutive twiddles instead of a power-of-two stride (bank conflicts).
+// n = 2^log2n held in shared memory (element e of column c at
+// buf[c*n + swz(e)]), input in bit-reversed order, output in natural order.
+// tw is the stage-major twiddle table (stage s at offset 2^(s-1) - 1), so
+// the lanes of a warp read consecutive twiddles instead of a power-of-two
+// stride (bank conflicts).
 __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restrict__ tw) {
   const int n = 1 << log2n;
   const int nb = (n >> 1) * ncol;
@@ -48,8 +59,9 @@ __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restr
       const int bb = b & ((n >> 1) - 1);
       const int grp = bb >> (s - 1);
       const int pos = bb & (half - 1);
-      const int a0 = col * n + (grp << s) + pos;
-      const int a1 = a0 + half;
+      const int e0 = (grp << s) + pos;
+      const int a0 = col * n + swz(e0, log2n);
+      const int a1 = col * n + swz(e0 + half, log2n);
       const float2 w = tws[pos];
       const float2 t = cmul(w, buf[a1]);
       const float2 x0 = buf[a0];
@@ -65,7 +77,7 @@ __device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restr
 __device__ __forceinline__ void xt_pixel(const XtSource& xs, float x, int64_t MN, int64_t q,
                                          float& i0, float& al) {
   const float v0 = fmaf(x, xs.xicom[q], xs.pcom[q]);
-  i0 = (xs.positivity && !((double)v0 > xs.floor_cmp)) ? xs.floor_val : v0;
+  i0 = (xs.positivity && !(v0 > xs.floor_cmp)) ? xs.floor_val : v0;
   al = fmaf(x, xs.xicom[MN + q], xs.pcom[MN + q]);
 }
 
@@ -146,12 +158,12 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
     const float a = attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
     float v = inu * a * sp.fg_scale;
     if (sp.gcf) v *= sp.gcf[q];  // apply_GCF, src/functions.cu:2468
-    buf[bitrev(j, sp.log2n)] = make_float2(v, 0.0f);
+    buf[swz(bitrev(j, sp.log2n), sp.log2n)] = make_float2(v, 0.0f);
   }
   __syncthreads();
   smem_fft(buf, sp.log2n, 1, tw);
   float2* out = grid + (int64_t)c * sp.MN + (int64_t)n * i;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[j];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[swz(j, sp.log2n)];
 }
 
 // Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate
@@ -168,7 +180,7 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __
   for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
-    buf[cc * n + bitrev(r, log2n)] = G[(int64_t)n * r + j0 + cc];
+    buf[cc * n + swz(bitrev(r, log2n), log2n)] = G[(int64_t)n * r + j0 + cc];
   }
   __syncthreads();
   smem_fft(buf, log2n, cb, tw);
@@ -182,7 +194,7 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __
     const float phase = -2.0f * (u + v);
     float s, co;
     sincospif(phase, &s, &co);
-    G[(int64_t)n * r + j] = cmul(buf[cc * n + r], make_float2(co, s));
+    G[(int64_t)n * r + j] = cmul(buf[cc * n + swz(r, log2n)], make_float2(co, s));
   }
 }
 
@@ -241,7 +253,7 @@ __global__ void __launch_bounds__(256) k_degrid(
   const ChanRange rg = ranges[c];
   const float2* __restrict__ G = grid + (int64_t)c * MN;
   const int nm1 = N - 1;
-  double acc = 0.0;
+  CompSum acc;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
        k += (int64_t)gridDim.x * blockDim.x) {
     const float4 d = __ldcs(deg + rg.off + k);
@@ -259,7 +271,7 @@ __global__ void __launch_bounds__(256) k_degrid(
     const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
     const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
     const float rr = o.x - mr, ri = o.y - mi;
-    acc += (double)(d.w * (rr * rr + ri * ri));
+    acc.add(d.w * (rr * rr + ri * ri));
     if (store) {
       const float2 cv = make_float2(d.w * rr, d.w * ri);
       __stcs(cvr + rg.off + k, cv);
@@ -270,8 +282,8 @@ __global__ void __launch_bounds__(256) k_degrid(
     for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, s));
     if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(cmax, __float_as_uint(mx));
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = acc;
+  const double bsum = block_sum(acc.value());
+  if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = bsum;
   if (last_block_done(done, gridDim.x * gridDim.y)) {
     finish_chi2(gridDim.y, gridDim.x, part, part_stride, nvis, normalize, chi2_out);
     if (threadIdx.x == 0) {
@@ -444,15 +456,15 @@ __global__ void __launch_bounds__(256) k_prior_values(PriorSet<Img> ps,
   const PriorParams pp = ps.pp[t];
   Img I = ps.img[t];
   I.bind();
-  double acc = 0.0;
+  CompSum acc;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
        q += (int64_t)gridDim.x * blockDim.x) {
     if (!(mask[q] & kMaskIn)) continue;
     const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
-    acc += (double)prior_pixel(pp, I, i, j);
+    acc.add(prior_pixel(pp, I, i, j));
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) ps.part[t][blockIdx.x] = acc;
+  const double bsum = block_sum(acc.value());
+  if (threadIdx.x == 0) ps.part[t][blockIdx.x] = bsum;
   if (last_block_done(done, gridDim.x * gridDim.y)) {
     for (int u = 0; u < ps.n; u++) {
       double v = 0.0;

@@ -77,26 +77,27 @@ __device__ double block_max_d(double v) {
 // evaluateXt / evaluateXtNoPositivity, src/functions.cu:2832-2864
 // (x from x_dev when it is set: the device line search's point)
 __global__ void k_eval_xt(int64_t MN, float x, const float* __restrict__ x_dev, float floor_val,
-                          double floor_cmp, int positivity, const float* __restrict__ pcom,
+                          float floor_cmp, int positivity, const float* __restrict__ pcom,
                           const float* __restrict__ xicom, float* __restrict__ xt) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= 2 * MN) return;
   if (x_dev) x = *x_dev;
   const float v = fmaf(x, xicom[q], pcom[q]);
-  xt[q] = (q < MN && positivity && !((double)v > floor_cmp)) ? floor_val : v;
+  xt[q] = (q < MN && positivity && !(v > floor_cmp)) ? floor_val : v;
 }
 
 // newP / newPNoPositivity, src/functions.cu:2779-2812
-// (xmin from xmin_dev when it is set: the device line search's minimum)
+// (xmin from xmin_dev when it is set: the device line search's minimum;
+// floor_cmp = float_below of the reference's FP64 threshold)
 __global__ void k_new_p(int64_t MN, float xmin, const float* __restrict__ xmin_dev,
-                        float floor_val, double floor_cmp, int positivity, float* __restrict__ p,
+                        float floor_val, float floor_cmp, int positivity, float* __restrict__ p,
                         float* __restrict__ xi) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= 2 * MN) return;
   if (xmin_dev) xmin = *xmin_dev;
   const float s = xi[q] * xmin;
   if (q < MN && positivity) {
-    if ((double)(p[q] + s) > floor_cmp) {
+    if (p[q] + s > floor_cmp) {
       p[q] += s;
       xi[q] = s;
     } else {
@@ -142,15 +143,16 @@ __global__ void __launch_bounds__(256) k_cg_stats(int64_t n, float den,
                                                   double* __restrict__ part, int stride,
                                                   uint32_t* __restrict__ done,
                                                   double* __restrict__ out) {
-  double gg = 0.0, dgg = 0.0;
+  CompSum ggs, dggs;
   float gmax = FLT_MIN;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
     const float x = xi[q], gq = g[q];
     gmax = fmaxf(gmax, fabsf(x) * fmaxf(fabsf(p[q]), 1.0f) / den);
-    gg += (double)(gq * gq);
-    dgg += (double)((x + gq) * x);
+    ggs.add(gq * gq);
+    dggs.add((x + gq) * x);
   }
+  double gg = ggs.value(), dgg = dggs.value();
   __shared__ double s1[32], s2[32];
   __shared__ float s3[32];
   gg = warp_sum_d(gg);
@@ -194,16 +196,18 @@ __global__ void __launch_bounds__(256) k_cg_stats(int64_t n, float den,
   }
 }
 
-// FP64 dot product partials of two float vectors
+// Dot product of two float vectors: the float products, summed per thread
+// (compensated), then in FP64
 __global__ void __launch_bounds__(256) k_dot(int64_t n, const float* __restrict__ a,
                                              const float* __restrict__ b,
                                              double* __restrict__ part,
                                              uint32_t* __restrict__ done,
                                              double* __restrict__ out) {
-  double s = 0.0;
+  CompSum cs;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x)
-    s += (double)(a[q] * b[q]);
+    cs.add(a[q] * b[q]);
+  double s = cs.value();
   __shared__ double sh[32];
   s = warp_sum_d(s);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
@@ -368,7 +372,7 @@ LsCache& ls_cache(Problem& P) {
 
 gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
                          const float* xicom, float* xt, int flag, int positivity, float floor_val,
-                         double floor_cmp, const LsTerms& terms, cudaGraphExec_t* out,
+                         float floor_cmp, const LsTerms& terms, cudaGraphExec_t* out,
                          int64_t* body_launches) {
   if (!c.cap) GV_CUDA(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
   if (!c.side) GV_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
@@ -453,7 +457,8 @@ class Solver {
   Solver(Problem& P, const gv_opt_desc& o) : P_(P), o_(o) {
     MN_ = (int64_t)P.M * P.N;
     floor_val_ = -1.0f * P.eta * P.minpix;
-    floor_cmp_ = -1.0 * P.eta * P.minpix;
+    // the reference compares against -eta * minpix in FP64
+    floor_cmp_ = float_below(-1.0 * P.eta * P.minpix);
   }
 
   gv_status init() {
@@ -954,7 +959,7 @@ class Solver {
   gv_opt_desc o_;
   int64_t MN_;
   float floor_val_;
-  double floor_cmp_;
+  float floor_cmp_;
   Workspace w_{};
   float* d_y_ = nullptr;
   float* d_s_ = nullptr;
