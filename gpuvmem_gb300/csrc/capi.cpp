@@ -205,7 +205,8 @@ gv_status gv_objective(gv_problem* p, float* d_img, int32_t flag_opt, double* f,
   GV_CHECK_PROBLEM(p);
   Problem& P = p->P;
   if (!d_img || !f) { gv::set_error("null image or output"); return GV_ERR_INVALID; }
-  gv_status s = gv::objective_launch(P, d_img, flag_opt, true);
+  gv_status s = P.use_graphs ? gv::eval_graph(P, d_img, nullptr, 0, flag_opt, 1, true)
+                             : gv::objective_launch(P, d_img, flag_opt, true);
   if (s != GV_OK) return s;
   s = gv::fetch_scalars(P, gv::kSlotTerm0 + (int)P.terms.size());
   if (s != GV_OK) return s;

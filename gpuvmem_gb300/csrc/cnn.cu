@@ -530,6 +530,11 @@ struct UNet {
   cudaStream_t stream = nullptr;
   int num_sms = 0;
   std::vector<void*> allocs;
+  // forward passes captured as CUDA graphs, one per batch size (the pass
+  // only reads and writes the network's own buffers, so a graph stays valid)
+  std::vector<cudaGraphExec_t> fwd_exec;
+  std::vector<int64_t> fwd_launches;
+  cudaStream_t cap = nullptr;
 
   int C(int l) const { return c0 << l; }
   int S(int l) const { return H >> l; }
@@ -542,6 +547,9 @@ struct UNet {
     return GV_OK;
   }
   ~UNet() {
+    for (cudaGraphExec_t g : fwd_exec)
+      if (g) cudaGraphExecDestroy(g);
+    if (cap) cudaStreamDestroy(cap);
     for (void* p : allocs) cudaFree(p);
     if (h_loss) cudaFreeHost(h_loss);
   }
@@ -645,10 +653,53 @@ struct UNet {
   View dec_view(int l) const { return l == L - 1 ? enc_view(l) : View{dec[l], C(l), 0}; }
   View ddec_view(int l) const { return l == L - 1 ? denc_view(l) : View{ddec[l], C(l), 0}; }
 
+  // The input is copied into the network's buffer, then the pass is one
+  // graph launch (captured on first use for this batch size on a private
+  // stream; a batch-1 pass is some 40 small kernels whose launch latency
+  // would otherwise set its time).
   gv_status forward(const float* d_in, int B) {
-    const Ctx c = ctx();
     GV_CUDA(cudaMemcpyAsync(in[0], d_in, sizeof(float) * B * cin * H * W,
                             cudaMemcpyDeviceToDevice, stream));
+    if (fwd_exec.empty()) {
+      fwd_exec.assign(maxB + 1, nullptr);
+      fwd_launches.assign(maxB + 1, 0);
+    }
+    if (!fwd_exec[B]) {
+      if (!cap) GV_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+      const cudaStream_t saved = stream;
+      const int64_t l0 = gv_launch_count();
+      stream = cap;
+      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed);
+      if (e != cudaSuccess) {
+        stream = saved;
+        return cuda_fail(e, "cudaStreamBeginCapture (U-Net forward)");
+      }
+      const gv_status s = forward_pass(B);
+      cudaGraph_t g = nullptr;
+      e = cudaStreamEndCapture(cap, &g);
+      stream = saved;
+      const int64_t nl = gv_launch_count() - l0;
+      add_launches(-nl);  // counted again at each replay
+      if (s != GV_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (U-Net forward)");
+      cudaGraphExec_t x = nullptr;
+      e = cudaGraphInstantiate(&x, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (U-Net forward)");
+      fwd_exec[B] = x;
+      fwd_launches[B] = nl;
+    }
+    GV_CUDA(cudaGraphLaunch(fwd_exec[B], stream));
+    add_launches(fwd_launches[B]);
+    return GV_OK;
+  }
+
+  // the forward pass on the network's input buffer in[0]
+  gv_status forward_pass(int B) {
+    const Ctx c = ctx();
     for (int l = 0; l < L; l++) {
       const int s = S(l), ci = l == 0 ? cin : C(l - 1);
       const Layer& l1 = layers[enc_layer(l, 0)];

@@ -178,10 +178,14 @@ gv_status gv_prior_gradient(gv_problem* p, int32_t term, const float* d_img,
 /* ObjectiveFunction::calcFunction: sum of lambda*term over the kept terms;
  * priors contribute only after gv_gradient was called with iter > 0 (the
  * reference's Fi::iteration).  fi_values (may be NULL) receives each
- * term's value before lambda. */
+ * term's value before lambda.  With graphs on (gv_problem_set_graphs) the
+ * kernels are captured on the first call per (d_img, flag_opt, prior
+ * gating) and replayed afterwards, as in gv_evaluate (the 8 most recently
+ * used keys are kept; results equal the launch-by-launch ones bit for bit). */
 gv_status gv_objective(gv_problem* p, float* d_img, int32_t flag_opt,
                        double* f, double* fi_values);
-/* ObjectiveFunction::calcGradient into d_xi (2*M*N, device). */
+/* ObjectiveFunction::calcGradient into d_xi (2*M*N, device); replayed from
+ * a graph per (d_img, d_xi, flag_opt, iter > 0) when graphs are on. */
 gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
                       int32_t flag_opt);
 
@@ -219,9 +223,11 @@ gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img,
 gv_status gv_evaluate(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
                       int32_t flag_opt, double* f, double* fi_values);
 
-/* 1 (default, or GV_GRAPHS unset/not "0" at creation): the optimiser's
- * objective evaluations are replayed from CUDA graphs; 0: launched kernel by
- * kernel.  Results are identical either way. */
+/* 1 (default, or GV_GRAPHS unset/not "0" at creation): gv_objective,
+ * gv_gradient and the optimiser's evaluations are replayed from CUDA
+ * graphs; 0: launched kernel by kernel.  Results are identical either way.
+ * The first call per key must not happen while the problem's stream is
+ * being captured. */
 gv_status gv_problem_set_graphs(gv_problem* p, int32_t enable);
 
 /* gv_optimize that also stops (exit_reason 4) once a line search from the

@@ -50,6 +50,28 @@ def test_evaluate_matches_objective_then_gradient():
         assert n1 - n0 == n2 - n1 > 0  # replays count their kernels
 
 
+def test_gradient_graph_matches_direct_launches():
+    """gv_gradient replays a captured gradient (factor pass, DChi2 GEMM,
+    split-K reduction, prior gradients) when graphs are on; the result is
+    the launch-by-launch one bit for bit, at both gating states."""
+    import torch
+    import gpuvmem_gb300 as gv
+    data, terms = _problem(n=256, nchan=2, seed=13)
+    pa = gv.Problem(data, terms)
+    pb = gv.Problem(data, terms)
+    pb.set_graphs(False)
+    for step, it in enumerate([0, 1, 2]):
+        img = _image(pa, 200 + step)
+        ia, ib = img.clone(), img.clone()
+        xa = torch.zeros_like(img)
+        xb = torch.zeros_like(img)
+        pa.objective(ia)
+        pb.objective(ib)
+        pa.gradient(ia, it, xi=xa)
+        pb.gradient(ib, it, xi=xb)
+        assert torch.equal(xa, xb), step
+
+
 @pytest.mark.parametrize("method", ["CG-FRPRMN", "CG-LBFGS"])
 def test_optimizer_with_and_without_graphs(method):
     import gpuvmem_gb300 as gv
