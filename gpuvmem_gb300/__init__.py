@@ -130,6 +130,7 @@ def lib():
         "gv_prior_value": [vp, i32, vp, f64p],
         "gv_prior_gradient": [vp, i32, vp, vp],
         "gv_objective": [vp, vp, i32, f64p, f64p],
+        "gv_objective_many": [vp, C.POINTER(vp), i32, i32, f64p, f64p],
         "gv_gradient": [vp, vp, vp, i32, i32],
         "gv_evaluate": [vp, vp, vp, i32, i32, f64p, f64p],
         "gv_problem_set_graphs": [vp, i32],
@@ -319,6 +320,16 @@ class Problem:
         fi = (C.c_double * 8)()
         check(lib().gv_objective(self.h, _ptr(img), flag_opt, C.byref(f), fi))
         return f.value, list(fi)[:len(self.terms)]
+
+    def objective_many(self, imgs, flag_opt=0):
+        """objective() of every image in imgs ([n, 2, N, M] or a list of
+        [2, N, M]) with one synchronisation; the images are not clipped.
+        Returns the n values of f."""
+        n = len(imgs)
+        ptrs = (C.c_void_p * n)(*[imgs[i].data_ptr() for i in range(n)])
+        f = (C.c_double * max(n, 1))()
+        check(lib().gv_objective_many(self.h, ptrs, n, flag_opt, f, None))
+        return [f[i] for i in range(n)]
 
     def gradient(self, img, it, flag_opt=0, xi=None):
         if xi is None:

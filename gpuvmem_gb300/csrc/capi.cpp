@@ -4,6 +4,7 @@
 // include/classes/fi.cuh:68-81, src/mfs.cu:117-140).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -218,6 +219,44 @@ gv_status gv_objective(gv_problem* p, float* d_img, int32_t flag_opt, double* f,
   }
   *f = tot;
   return GV_OK;
+}
+
+gv_status gv_objective_many(gv_problem* p, const float* const* d_imgs, int32_t count,
+                            int32_t flag_opt, double* f, double* fi_values) {
+  GV_CHECK_PROBLEM(p);
+  Problem& P = p->P;
+  if (!d_imgs || !f || count < 0) { gv::set_error("invalid image list or output"); return GV_ERR_INVALID; }
+  for (int32_t i = 0; i < count; i++)
+    if (!d_imgs[i]) { gv::set_error("null image in the list"); return GV_ERR_INVALID; }
+  const int nt = (int)P.terms.size();
+  const size_t need = (size_t)count * (size_t)nt;
+  if (P.h_many_cap < need) {
+    if (P.h_many) cudaFreeHost(P.h_many);
+    P.h_many = nullptr;
+    P.h_many_cap = 0;
+    GV_CUDA(cudaMallocHost(&P.h_many, sizeof(double) * std::max<size_t>(need, 1)));
+    P.h_many_cap = need;
+  }
+  const size_t bytes = sizeof(float) * 2 * (size_t)P.M * (size_t)P.N;
+  for (int32_t i = 0; i < count; i++) {
+    GV_CUDA(cudaMemcpyAsync(P.d_tmp, d_imgs[i], bytes, cudaMemcpyDeviceToDevice, P.stream));
+    gv_status s = P.use_graphs ? gv::eval_graph(P, P.d_tmp, nullptr, 0, flag_opt, 1, false)
+                               : gv::objective_launch(P, P.d_tmp, flag_opt, false);
+    if (s != GV_OK) return s;
+    GV_CUDA(cudaMemcpyAsync(P.h_many + (size_t)i * nt, P.d_scal + gv::kSlotTerm0,
+                            sizeof(double) * nt, cudaMemcpyDeviceToHost, P.stream));
+  }
+  GV_CUDA(cudaStreamSynchronize(P.stream));
+  for (int32_t i = 0; i < count; i++) {
+    double tot = 0.0;
+    for (int t = 0; t < nt; t++) {
+      const double v = P.h_many[(size_t)i * nt + t];
+      if (fi_values) fi_values[(size_t)i * nt + t] = v;
+      tot += (double)P.terms[t].lambda * v;
+    }
+    f[i] = tot;
+  }
+  return gv::check_device_error(P);
 }
 
 gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter, int32_t flag_opt) {

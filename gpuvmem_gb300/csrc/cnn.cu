@@ -103,10 +103,15 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm(Op op, int M, int N, int 
       const int og = idx & (kBM / 8 - 1), kk = idx / (kBM / 8);
       const int k = k0 + kk;
       float v[8];
+      const int mg = m0 + og * 8;
+      if (k < kend && mg + 7 < M && op.rows8()) {
+        op.a8(mg, k, v);
+      } else {
 #pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const int m = m0 + og * 8 + i;
-        v[i] = (k < kend && m < M) ? op.a(m, k) : 0.0f;
+        for (int i = 0; i < 8; i++) {
+          const int m = mg + i;
+          v[i] = (k < kend && m < M) ? op.a(m, k) : 0.0f;
+        }
       }
       *reinterpret_cast<uint4*>(sa + tile_off(og >> 3, og & 7, kk, L::kSboA)) =
           make_uint4(bf16x2(v[0], v[1]), bf16x2(v[2], v[3]), bf16x2(v[4], v[5]),
@@ -199,6 +204,22 @@ struct ConvFwdOp {
     if ((unsigned)yy >= (unsigned)H || (unsigned)xx >= (unsigned)W) return 0.0f;
     return x[((size_t)(b * xC + xc0 + cin) * H + yy) * W + xx];
   }
+  // a(m + i, k) for i < 8, when rows m..m+7 are in one image row (rows8):
+  // the index arithmetic once for the eight
+  __device__ bool rows8() const { return (W & 7) == 0; }
+  __device__ void a8(int m, int k, float* v) const {
+    const int HW = H * W;
+    const int b = m / HW, r = m - b * HW, y0 = r / W, x0 = r - y0 * W;
+    const int kk = ks * ks, cin = k / kk, t = k - cin * kk;
+    const int yy = y0 + t / ks - ks / 2, dx = t % ks - ks / 2;
+    const bool rowok = (unsigned)yy < (unsigned)H;
+    const float* row = x + ((size_t)(b * xC + xc0 + cin) * H + (rowok ? yy : 0)) * W;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int xx = x0 + i + dx;
+      v[i] = (rowok && (unsigned)xx < (unsigned)W) ? row[xx] : 0.0f;
+    }
+  }
   __device__ float b(int k, int n) const { return w[(size_t)n * Cin * ks * ks + k]; }
   __device__ void store(int m, int n, float v, int split) const {
     if (part) {
@@ -244,6 +265,20 @@ struct ConvBwdDataOp {
     if ((unsigned)yy >= (unsigned)H || (unsigned)xx >= (unsigned)W) return 0.0f;
     return dz[((size_t)(b * zC + zc0 + co) * H + yy) * W + xx];
   }
+  __device__ bool rows8() const { return (W & 7) == 0; }
+  __device__ void a8(int m, int k, float* v) const {
+    const int HW = H * W;
+    const int b = m / HW, r = m - b * HW, y0 = r / W, x0 = r - y0 * W;
+    const int kk = ks * ks, co = k / kk, t = k - co * kk;
+    const int yy = y0 - t / ks + ks / 2, dx = -(t % ks) + ks / 2;
+    const bool rowok = (unsigned)yy < (unsigned)H;
+    const float* row = dz + ((size_t)(b * zC + zc0 + co) * H + (rowok ? yy : 0)) * W;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int xx = x0 + i + dx;
+      v[i] = (rowok && (unsigned)xx < (unsigned)W) ? row[xx] : 0.0f;
+    }
+  }
   __device__ float b(int k, int n) const {
     const int kk = ks * ks, co = k / kk, t = k - co * kk;
     return w[((size_t)co * Cin + n) * kk + t];
@@ -273,6 +308,8 @@ struct ConvBwdWeightOp {
     if ((unsigned)yy >= (unsigned)H || (unsigned)xx >= (unsigned)W) return 0.0f;
     return x[((size_t)(b * xC + xc0 + cin) * H + yy) * W + xx];
   }
+  __device__ bool rows8() const { return false; }  // rows are (cin, tap) pairs
+  __device__ void a8(int, int, float*) const {}
   __device__ float b(int k, int n) const {
     const int HW = H * W;
     const int b = k / HW, r = k - b * HW;

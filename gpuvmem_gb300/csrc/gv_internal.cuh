@@ -120,6 +120,8 @@ struct Problem {
   int part_stride = 0;           // partials per channel / term
   double* d_scal = nullptr;      // [kNumScal]
   double* h_scal = nullptr;      // pinned mirror
+  double* h_many = nullptr;      // pinned term values of gv_objective_many
+  size_t h_many_cap = 0;         // doubles h_many holds
   float* d_tmp = nullptr;        // [2*MN] scratch image (dchi2 channel etc.)
   float* d_opt = nullptr;        // optimiser workspace (allocated on demand)
   size_t opt_bytes = 0;

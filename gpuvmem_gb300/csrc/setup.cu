@@ -198,6 +198,7 @@ void free_problem(Problem& P) {
   cudaFree(P.d_flags);
   cudaFree(P.tc_partial);
   if (P.h_scal) cudaFreeHost(P.h_scal);
+  if (P.h_many) cudaFreeHost(P.h_many);
   graph_cache_free(P);
   ls_cache_free(P);
   cudaFree(P.d_ls);

@@ -150,17 +150,12 @@ def choose_start(sky: Sky, net: UNet, scales=SCALES, cuts=CUTS):
     cands = warm[None, None].repeat(len(cuts), len(scales), 1, 1, 1)    # [cuts, scales, 2, H, W]
     cands[:, :, 0] = sky.floor + sc * kept[:, None]
     flat = cands.view(-1, *warm.shape)
-    # one scratch image for every candidate (the objective clips the image
-    # it evaluates, and one buffer replays one captured evaluation)
-    work = torch.empty_like(warm)
-    fs = []
-    for i in range(flat.shape[0]):
-        work.copy_(flat[i])
-        fs.append(sky.prob.objective(work)[0])
+    # the candidates and the plain start scored with one synchronisation
+    # (each evaluated in the problem's scratch image, so none is clipped)
+    scores = sky.prob.objective_many(list(flat) + [plain])
+    fs, fp = scores[:-1], scores[-1]
     i_best = min(range(len(fs)), key=lambda i: (fs[i] if fs[i] == fs[i] else float("inf"), i))
     best, fw = flat[i_best].clone(), fs[i_best]
-    work.copy_(plain)
-    fp, _ = sky.prob.objective(work)
     sky.prob.set_iteration(0)
     return (best, "warm", fw, fp) if fw <= fp else (plain, "plain", fw, fp)
 

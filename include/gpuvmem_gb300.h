@@ -184,6 +184,14 @@ gv_status gv_prior_gradient(gv_problem* p, int32_t term, const float* d_img,
  * used keys are kept; results equal the launch-by-launch ones bit for bit). */
 gv_status gv_objective(gv_problem* p, float* d_img, int32_t flag_opt,
                        double* f, double* fi_values);
+/* calcFunction of `count` images (d_imgs: a host array of device pointers,
+ * each 2*M*N floats) with one host synchronisation for all of them (no
+ * counterpart in the reference: scores candidate starting images).  Each
+ * image is copied into the problem's scratch image and evaluated there, so
+ * the images themselves are not clipped; f[i] (and, if not NULL,
+ * fi_values[i * nterms + t]) equal what gv_objective returns for image i. */
+gv_status gv_objective_many(gv_problem* p, const float* const* d_imgs, int32_t count,
+                            int32_t flag_opt, double* f, double* fi_values);
 /* ObjectiveFunction::calcGradient into d_xi (2*M*N, device); replayed from
  * a graph per (d_img, d_xi, flag_opt, iter > 0) when graphs are on. */
 gv_status gv_gradient(gv_problem* p, float* d_img, float* d_xi, int32_t iter,

@@ -72,6 +72,23 @@ def test_gradient_graph_matches_direct_launches():
         assert torch.equal(xa, xb), step
 
 
+def test_objective_many_matches_objective():
+    """gv_objective_many scores a list of images with one synchronisation;
+    each value equals gv_objective's, and the listed images stay unclipped."""
+    import torch
+    import gpuvmem_gb300 as gv
+    data, terms = _problem(n=128, nchan=2, seed=17)
+    pa = gv.Problem(data, terms)
+    pa.set_iteration(1)
+    imgs = torch.stack([_image(pa, 300 + k) for k in range(5)])
+    before = imgs.clone()
+    fm = pa.objective_many(imgs)
+    assert torch.equal(imgs, before)
+    for k in range(imgs.shape[0]):
+        f, _ = pa.objective(imgs[k].clone())
+        assert fm[k] == f, (k, fm[k], f)
+
+
 @pytest.mark.parametrize("method", ["CG-FRPRMN", "CG-LBFGS"])
 def test_optimizer_with_and_without_graphs(method):
     import gpuvmem_gb300 as gv
