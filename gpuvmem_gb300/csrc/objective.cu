@@ -9,8 +9,9 @@
 //   2. k_cols_fft   column pass of the FFT, with phase_rotate applied on the
 //                   way out;
 //   3. k_degrid     vis_mod + residual + chi2Vector + reduction: one stream
-//                   over the cell-sorted visibilities, FP64 partial sums,
-//                   weighted residuals stored for DChi2.
+//                   over the cell-sorted visibilities, compensated per-thread
+//                   sums combined in FP64, weighted residuals stored for
+//                   DChi2.
 //
 // No per-call allocation, no host synchronisation except the single scalar
 // read-back at the end of an evaluation.
@@ -529,7 +530,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.gcf = P.d_gcf;
   sp.beam_x = P.d_beam_x;
   sp.beam_y = P.d_beam_y;
-  sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0, 0};
+  sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0f, 0};
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
   const size_t sm1 = sizeof(float2) * (2 * n - 1);
   if (sm1 > 48 * 1024)
