@@ -47,3 +47,22 @@ def test_version_and_error_without_gpu():
     assert L.gv_problem_create(None, ctypes.byref(h)) == 1
     assert b"null" in L.gv_last_error()
     assert L.gv_problem_destroy(None) == 0
+
+
+def test_null_handles_are_rejected_without_gpu():
+    """Every problem entry point validates its handle before touching the
+    GPU: a null handle is GV_ERR_INVALID with a message, never a crash."""
+    import gpuvmem_gb300 as gv
+    L = gv.lib()
+    f = ctypes.c_double()
+    calls = [
+        lambda: L.gv_objective(None, None, 0, ctypes.byref(f), None),
+        lambda: L.gv_objective_many(None, None, 0, 0, ctypes.byref(f), None),
+        lambda: L.gv_gradient(None, None, None, 0, 0),
+        lambda: L.gv_evaluate(None, None, None, 0, 0, ctypes.byref(f), None),
+        lambda: L.gv_dchi2(None, None, 0, None),
+        lambda: L.gv_problem_set_graphs(None, 1),
+    ]
+    for call in calls:
+        assert call() == 1
+        assert b"null" in L.gv_last_error()
