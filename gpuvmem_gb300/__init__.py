@@ -325,7 +325,14 @@ class Problem:
         """objective() of every image in imgs ([n, 2, N, M] or a list of
         [2, N, M]) with one synchronisation; the images are not clipped.
         Returns the n values of f."""
+        import torch
         n = len(imgs)
+        for i in range(n):
+            t = imgs[i]
+            if (t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous()
+                    or t.numel() != 2 * self.N * self.M):
+                raise ValueError(f"image {i}: need a contiguous float32 CUDA tensor of "
+                                 f"2 x {self.N} x {self.M} values")
         ptrs = (C.c_void_p * n)(*[imgs[i].data_ptr() for i in range(n)])
         f = (C.c_double * max(n, 1))()
         check(lib().gv_objective_many(self.h, ptrs, n, flag_opt, f, None))

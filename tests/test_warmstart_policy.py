@@ -124,3 +124,25 @@ def test_nan_scores_never_win():
     start, which, fw, fp = W.choose_start(sky, FakeNet(pred))
     assert which == "warm" and fw == 5.0 and fp == 6.0
     torch.testing.assert_close(start, exp[-1], rtol=0, atol=1e-6)
+
+
+def test_summary_counts_only_skies_that_reach_the_target_in_both_runs():
+    rows = [
+        dict(t_plain=0.06, t_warm=0.02, reached_plain=True, reached_warm=True, start="warm",
+             it_plain=60, it_warm=20, t_warm_priors_first=0.015, reached_warm_priors_first=True),
+        dict(t_plain=0.04, t_warm=0.01, reached_plain=True, reached_warm=True, start="warm",
+             it_plain=40, it_warm=10, t_warm_priors_first=0.02, reached_warm_priors_first=True),
+        dict(t_plain=0.05, t_warm=0.05, reached_plain=True, reached_warm=True, start="plain",
+             it_plain=50, it_warm=50, t_warm_priors_first=0.05, reached_warm_priors_first=False),
+        # the warm run did not reach the target: left out of the warm statistics
+        dict(t_plain=0.30, t_warm=0.001, reached_plain=True, reached_warm=False, start="warm",
+             it_plain=300, it_warm=1, t_warm_priors_first=0.001, reached_warm_priors_first=True),
+    ]
+    s = W.summarize(rows)
+    assert s["skies"] == 4 and s["both_reached"] == 3 and s["warm_chosen"] == 3
+    assert s["speedup_median"] == pytest.approx(3.0)   # ratios 3, 4, 1
+    assert s["speedup_total"] == pytest.approx(0.15 / 0.08)
+    assert s["t_plain_median_s"] == pytest.approx(0.05)
+    assert s["it_plain_median"] == 50 and s["it_warm_median"] == 20
+    # priors-first: skies 1, 2 and 4 reach it (ratios 4, 2, 300)
+    assert s["speedup_median_priors_first"] == pytest.approx(4.0)
