@@ -249,6 +249,9 @@ class Problem:
         h = C.c_void_p()
         check(L.gv_problem_create(C.byref(desc), C.byref(h)))
         self.h = h
+        import torch
+        # the device the problem's buffers live on (the current one)
+        self.device = torch.device("cuda", torch.cuda.current_device())
         if stream is not None:
             self.set_stream(stream)
 
@@ -333,6 +336,8 @@ class Problem:
                     or t.numel() != 2 * self.N * self.M):
                 raise ValueError(f"image {i}: need a contiguous float32 CUDA tensor of "
                                  f"2 x {self.N} x {self.M} values")
+            if t.device != self.device:
+                raise ValueError(f"image {i} is on {t.device}, the problem on {self.device}")
         ptrs = (C.c_void_p * n)(*[imgs[i].data_ptr() for i in range(n)])
         f = (C.c_double * max(n, 1))()
         check(lib().gv_objective_many(self.h, ptrs, n, flag_opt, f, None))

@@ -11,10 +11,13 @@
 //
 // Set-up: the first call on a device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress and caches it for
-// that device; make that first call before any stream capture.  Every call
-// shares the array and leaves the last call's partials in it; each call
-// rewrites all the rows it uses, so nothing needs clearing, but calls that
-// overlap on the GPU (different streams, or another host thread) race on it.
+// that device; make that first call before any stream capture.  Later calls
+// outside a capture look the address up again (no allocation; it keeps the
+// cache valid after a cudaDeviceReset re-creates the context), calls inside
+// a capture use the cached address.  Every call shares the array and leaves
+// the last call's partials in it; each call rewrites all the rows it uses,
+// so nothing needs clearing, but calls that overlap on the GPU (different
+// streams, or another host thread) race on it.
 #include <mutex>
 
 #include "gv_internal.cuh"
@@ -31,7 +34,10 @@ constexpr int kMaxDevices = 64;
 double* g_partials_addr[kMaxDevices] = {};
 std::mutex g_partials_mu;
 
-gv_status partials_for_current_device(double** out) {
+// Device address of g_row_partials on the current device.  `capturing`:
+// the launch stream is being captured, so only the cached address is used
+// (a first look-up may load the module, which a capture does not allow).
+gv_status partials_for_current_device(bool capturing, double** out) {
   int dev = -1;
   GV_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) {
@@ -39,7 +45,12 @@ gv_status partials_for_current_device(double** out) {
     return GV_ERR_UNSUPPORTED;
   }
   std::lock_guard<std::mutex> lk(g_partials_mu);
-  if (g_partials_addr[dev] == nullptr) {
+  if (!capturing || g_partials_addr[dev] == nullptr) {
+    if (capturing) {
+      set_error("gv_prior_value_static: the first call on a device must come before any "
+                "stream capture (it looks up the static scratch's address)");
+      return GV_ERR_INVALID;
+    }
     void* p = nullptr;
     GV_CUDA(cudaGetSymbolAddress(&p, g_row_partials));
     g_partials_addr[dev] = static_cast<double*>(p);
@@ -112,14 +123,29 @@ __global__ void __launch_bounds__(256) k_prior_rows_static(RowPrior rp,
   }
 }
 
-// sum of the row partials in row order
-__global__ void k_sum_rows_static(int n, const double* __restrict__ partials,
-                                  double* __restrict__ out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < n; i++) s += partials[i];
-    *out = s;
+// Sum of the row partials in a fixed order: thread t adds rows
+// [t*k, (t+1)*k) with Neumaier's compensation (Neumaier 1974), then the
+// 256 compensated values are added pairwise in a fixed tree.  Deterministic
+// and accurate to a few FP64 ulps of the largest partial for 8192 rows.
+__global__ void __launch_bounds__(256) k_sum_rows_static(int n, const double* __restrict__ partials,
+                                                         double* __restrict__ out) {
+  __shared__ double red[256];
+  const int per = (n + 255) / 256;
+  const int lo = threadIdx.x * per, hi = min(n, lo + per);
+  double s = 0.0, c = 0.0;
+  for (int i = lo; i < hi; i++) {
+    const double x = partials[i];
+    const double t = s + x;
+    c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+    s = t;
   }
+  red[threadIdx.x] = s + c;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
 }
 
 }  // namespace
@@ -143,14 +169,28 @@ extern "C" gv_status gv_prior_value_static(int32_t kind, const float* d_plane,
                   "(the static scratch holds one partial per row)");
     return GV_ERR_UNSUPPORTED;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (st != nullptr) {
+    // the stream must belong to the current device: the scratch address
+    // and the launch are the current device's
+    int dev = -1, sdev = -1;
+    GV_CUDA(cudaGetDevice(&dev));
+    GV_CUDA(cudaStreamGetDevice(st, &sdev));
+    if (sdev != dev) {
+      gv::set_error("gv_prior_value_static: the stream belongs to another device than the "
+                    "current one");
+      return GV_ERR_INVALID;
+    }
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GV_CUDA(cudaStreamIsCapturing(st, &cap));
   double* partials = nullptr;
-  gv_status s = gv::partials_for_current_device(&partials);
+  gv_status s = gv::partials_for_current_device(cap != cudaStreamCaptureStatusNone, &partials);
   if (s != GV_OK) return s;
   gv::RowPrior rp{kind, n, noise_cut, prior_value, eta, epsilon};
-  cudaStream_t st = (cudaStream_t)stream;
   gv::k_prior_rows_static<<<n, 256, 0, st>>>(rp, d_plane, d_noise, partials);
   GV_LAUNCH("k_prior_rows_static");
-  gv::k_sum_rows_static<<<1, 32, 0, st>>>(n, partials, d_value);
+  gv::k_sum_rows_static<<<1, 256, 0, st>>>(n, partials, d_value);
   GV_LAUNCH("k_sum_rows_static");
   return GV_OK;
 }

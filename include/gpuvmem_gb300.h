@@ -278,9 +278,13 @@ gv_status gv_residuals(gv_problem* p, float* h_out);
  * GV_FI_LAPLACIAN; prior_value/eta/epsilon as gv_fi_desc.  The only scratch
  * is a library-owned static device array of one FP64 partial per row, so
  * n is limited to 8192 (GV_ERR_UNSUPPORTED beyond).  The first call on a
- * device looks up that array's address; make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU race.  Work is
- * enqueued on `stream` (cudaStream_t, NULL = legacy default stream). */
+ * device looks up that array's address; make it before any stream capture
+ * (a first call inside a capture returns GV_ERR_INVALID).  Calls outside a
+ * capture look the address up again, so a cudaDeviceReset in between does
+ * not leave a stale address.  Calls share the array: calls that overlap on
+ * the GPU race.  Work is enqueued on `stream` (cudaStream_t, NULL = legacy
+ * default stream), which must belong to the current device
+ * (GV_ERR_INVALID otherwise). */
 gv_status gv_prior_value_static(int32_t kind, const float* d_plane, const float* d_noise,
                                 float noise_cut, int32_t n, float prior_value, float eta,
                                 float epsilon, double* d_value, void* stream);

@@ -8,7 +8,7 @@
 # boost.  Outputs go to oracle/_ref/ only.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${GV_REFERENCE:-/root/reference}"
+REF="${GV_REFERENCE:?set GV_REFERENCE to the gpuvmem source tree}"
 OUT="$HERE/../_ref"
 mkdir -p "$OUT/gobj"
 FLAGS=(-std=c++17 -O2 -rdc=true -gencode arch=compute_103a,code=sm_103a

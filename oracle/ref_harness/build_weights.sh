@@ -6,7 +6,7 @@
 # replace casacore, cfitsio and boost.  Outputs go to oracle/_ref/ only.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${GV_REFERENCE:-/root/reference}"
+REF="${GV_REFERENCE:?set GV_REFERENCE to the gpuvmem source tree}"
 OUT="$HERE/../_ref"
 mkdir -p "$OUT/wobj"
 FLAGS=(-std=c++17 -O2 -x cu -I "$HERE/shim" -I "$REF/include" -I "$REF/include/classes"

@@ -448,6 +448,56 @@ int rr_dchi2(void* hh, const float* img, int flag_opt, float* out) {
   return 0;
 }
 
+// dchi2() restricted to image rows [i0, i0 + rows): the reference's DChi2
+// and DChi2_total_* kernels launched over the band only (pointers offset to
+// row i0, the DChi2 centres shifted by i0 rows; i0 and rows multiples of the
+// 16-row launch tile).  A full-size gradient of a large image takes the
+// reference's kernel tens of minutes; a band gives its values at those rows.
+// out: 2 planes x rows x N floats.
+int rr_dchi2_band(void* hh, const float* img, int flag_opt, int i0, int rows, float* out) {
+  Harness* h = (Harness*)hh;
+  long M = h->M, N = h->N;
+  const long MN = M * N;
+  if (i0 < 0 || rows <= 0 || i0 % 16 || rows % 16 || i0 + rows > N)
+    return fail("rr_dchi2_band: i0 and rows must be multiples of 16 inside the image");
+  RR_RT(cudaMemcpy(h->d_img, img, sizeof(float) * 2 * MN, cudaMemcpyHostToDevice));
+  RR_RT(cudaMemset(h->d_res, 0, sizeof(float) * 2 * MN));
+  const long off = (long)i0 * N;
+  for (auto& C : h->ch) {
+    if (C.nvis <= 0) continue;
+    RR_RT(cudaMemset(h->d_dchi2, 0, sizeof(float) * MN));
+    long nv = C.nvis;
+    float fg = h->fg_scale, nc = h->noise_cut, x = h->xobs, y = h->yobs - (float)i0;
+    double dx = h->DELTAX, dy = h->DELTAY;
+    float a = h->D, b = h->pbf, c = h->pbcut, f = C.freq;
+    int pbt = h->pb;
+    bool norm = h->normalize != 0;
+    float* noise = h->d_noise + off;
+    float* dch = h->d_dchi2 + off;
+    float* res = h->d_res + off;
+    float* im = h->d_img + off;
+    const dim3 grid(h->bNN.x, rows / 16);
+    RR_TRY(launch("dchi2", grid, h->tNN, 0,
+                  {&noise, &dch, &C.vr, &C.uvw, &C.w, &N, &nv, &fg, &nc, &x, &y, &x, &y, &dx,
+                   &dy, &a, &b, &c, &f, &pbt, &norm}));
+    RR_RT(cudaDeviceSynchronize());
+    float nu0 = h->nu_0, thr = h->threshold;
+    // the total kernels index plane 1 at M*N past their image pointers
+    if (flag_opt % 2 == 0) {
+      RR_TRY(launch("tot0", grid, h->tNN, 0,
+                    {&noise, &res, &dch, &im, &f, &nu0, &nc, &thr, &N, &M}));
+    } else {
+      RR_TRY(launch("tota", grid, h->tNN, 0,
+                    {&noise, &res, &dch, &im, &f, &nu0, &nc, &fg, &thr, &N, &M}));
+    }
+    RR_RT(cudaDeviceSynchronize());
+  }
+  for (int p = 0; p < 2; p++)
+    RR_RT(cudaMemcpy(out + (long)p * rows * N, h->d_res + p * MN + off, sizeof(float) * rows * N,
+                     cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 // Weighted residuals w*Vr of the last chi2, channel-major (2*V floats)
 int rr_residuals(void* hh, float* out) {
   Harness* h = (Harness*)hh;

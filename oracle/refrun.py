@@ -41,6 +41,7 @@ def lib():
         L.rr_prior.argtypes = [vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                f32p, f32p, f32p]
         L.rr_time.argtypes = [vp, f32p, C.c_int, C.c_int, f64p, f64p]
+        L.rr_dchi2_band.argtypes = [vp, f32p, C.c_int, C.c_int, C.c_int, f32p]
         L.rr_destroy.argtypes = [vp]
         _LIB = L
     return _LIB
@@ -106,6 +107,15 @@ class RefHarness:
         img = np.ascontiguousarray(img, dtype=np.float32)
         out = np.zeros((2, self.N, self.M), dtype=np.float32)
         _check(lib().rr_dchi2(self.h, _p(img, C.c_float), flag_opt, _p(out, C.c_float)))
+        return out
+
+    def dchi2_band(self, img, i0, rows, flag_opt=0):
+        """dchi2() over image rows [i0, i0 + rows) only (multiples of 16):
+        both result planes of those rows, (2, rows, N)."""
+        img = np.ascontiguousarray(img, dtype=np.float32)
+        out = np.zeros((2, rows, self.N), dtype=np.float32)
+        _check(lib().rr_dchi2_band(self.h, _p(img, C.c_float), flag_opt, int(i0), int(rows),
+                                   _p(out, C.c_float)))
         return out
 
     def residuals(self):
