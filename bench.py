@@ -11,15 +11,26 @@ synthetic data.
   e2e     the same through the public API (gpuvmem_gb300.Problem), the image
           copied in from pinned host memory and the gradient and objective
           read back every step;
-  roofline  the dominant kernel (tcgen05 DChi2) as TFLOP/s against the
-          measured dense BF16 peak / 3 (three FP16 products per algorithmic
-          multiply-add);
+  roofline  the dominant kernel (tcgen05 DChi2, timed inside the timed
+          loop as the gradient call) as TFLOP/s against the measured
+          sustained dense BF16 peak / 3 (three FP16 products per
+          algorithmic multiply-add; the gradient runs about a second per
+          launch inside a long loop);
+  reference_cuda  the reference's own CUDA kernels (compiled from its
+          sources, launched with its launch shapes and host sequence by the
+          harness in oracle/ref_harness) timed on the same GPU: chi2() in
+          full, dchi2() over a band of rows scaled to the image;
+  converge  the first half of the headline metric: wall time to an
+          objective within 1e-4 of the plain solver's converged value, from
+          the learned warm start (network forward pass and start policy
+          included) against the plain start, on held-out 256^2 skies;
   cpu_baseline  the CPU oracle (FP64 restatement of the reference's
           algorithm) on a bounded sample, scaled to evaluations/s.
 
 --impl reference times the reference's CPU implementation of this path.  The
 reference has none (its objective and gradient exist only as CUDA kernels),
-so the arm runs the oracle port with all host threads.
+so the arm runs the oracle port with all host threads; each step is a bounded
+sample (the full chi2 and DChi2 at a few pixels), scaled to one evaluation.
 """
 
 from __future__ import annotations
@@ -57,6 +68,11 @@ def parse():
     ap.add_argument("--case", default=None, help="run a profiling case instead of the bench")
     ap.add_argument("--autotune", action="store_true",
                     help="measure and keep the fastest launch shapes before timing")
+    ap.add_argument("--converge-skies", type=int, default=200,
+                    help="held-out skies of the warm-start measurement (0: skip)")
+    ap.add_argument("--ref-band-rows", type=int, default=16,
+                    help="image rows of the reference DChi2 band (configuration 1)")
+    ap.add_argument("--no-reference-cuda", action="store_true")
     return ap.parse_args()
 
 
@@ -92,6 +108,11 @@ class Clocks:
                                          stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            # a sample before the region starts (short regions end before the
+            # next 200 ms sample)
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 3.0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
@@ -102,6 +123,10 @@ class Clocks:
 
     def __exit__(self, *a):
         if self.proc:
+            # and one after it ends
+            n0, t0 = len(self.rows), time.time()
+            while len(self.rows) == n0 and time.time() - t0 < 1.0:
+                time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -128,15 +153,15 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profile_traffic(nvis):
-    """DRAM bytes per DChi2 launch: the ncu capture of the one-channel case
-    (profiles/dchi2_tc_traffic.json) scaled by the visibility count."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "dchi2_tc_traffic.json")) as f:
-            t = json.load(f)
-        return t["case_dram_bytes"] * nvis / t["case_visibilities"]
-    except Exception:
-        return None
+# DRAM bytes per visibility of one DChi2 launch (dram__bytes_read.sum +
+# dram__bytes_write.sum of k_dchi2_tc in an ncu capture of the one-channel
+# 2048^2 case, `bench.py --case dchi2_2048_1ch`, divided by its
+# visibilities).  The traffic of the full launch is this times its
+# visibilities: the operands are generated on chip, so the traffic is the
+# visibility constants re-read per output tile plus the partial images.
+DCHI2_DRAM_BYTES_PER_VIS = 268.33
+DCHI2_TRAFFIC_SOURCE = ("ncu capture of k_dchi2_tc, one channel of 2048^2 (bench.py --case "
+                        "dchi2_2048_1ch), scaled by the visibility count")
 
 
 def cpu_baseline(data, terms, sample_s, impl_kind="port"):
@@ -175,6 +200,11 @@ def cpu_baseline(data, terms, sample_s, impl_kind="port"):
 
 
 def run_reference(args):
+    """The FP64 oracle port on the host cores (the reference has no CPU
+    implementation of this path).  Each step is one bounded sample -- the
+    full chi2 of every channel and DChi2 at mask pixels of channel 0 for a
+    fixed time -- scaled to one full evaluation; ms_per_step is the
+    sample's own wall time, ms_per_eval the scaled figure."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -182,23 +212,83 @@ def run_reference(args):
         raise SystemExit("--impl reference covers configurations 0-2")
     cfg, terms = workload(args.config)
     data = synth.generate(cfg, device=None if args.config == 0 else _gen_device())
-    times = []
+    per_eval, walls = [], []
     base = None
     for s in range(args.warmup + args.steps):
+        t0 = time.time()
         b = cpu_baseline(data, terms, max(2.0, args.cpu_sample_s / max(1, args.steps)))
         if s >= args.warmup:
-            times.append(1.0 / b["value"])
+            per_eval.append(1.0 / b["value"])
+            walls.append(time.time() - t0)
             base = b
-    v = args.steps / sum(times)
+    v = args.steps / sum(per_eval)
     line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(walls) / args.steps,
+            "ms_per_eval": 1e3 * sum(per_eval) / args.steps,
+            "step": "one bounded sample (full chi2 + DChi2 at a few mask pixels), scaled to "
+                    "one evaluation for value",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (FP64 oracle port; the reference computes this path in FP32 on the GPU)",
             "data": "synthetic", "config": config_desc(cfg, data), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": base["cores"],
                              "kind": "port", "sample": base["sample"]},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda(data, img, band_rows):
+    """The reference's own kernels on this GPU (oracle/ref_harness): device
+    time of chi2() (src/functions.cu:4323-4454) and of dchi2()
+    (:4456-4558); dchi2 over a band of rows at the image centre, scaled by
+    N / rows when the band is not the whole image (every row of the
+    benchmark images lies inside the mask, so rows cost alike)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import refrun
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"harness import failed: {e}"}
+    if not refrun.available():
+        return {"unavailable": "reference kernels (oracle/_ref/ref_kernels.cubin) or the "
+                               "harness library are not built"}
+    rows = max(16, min(data.N, band_rows) // 16 * 16)
+    ref = refrun.RefHarness(data)
+    try:
+        ms_chi2, ms_band = ref.time(img, reps=3 if rows == data.N else 1, band_rows=rows)
+    finally:
+        ref.close()
+    ms_dchi2 = ms_band * data.N / rows
+    return {"evals_per_s": 1e3 / (ms_chi2 + ms_dchi2), "chi2_ms": ms_chi2, "dchi2_ms": ms_dchi2,
+            "dchi2_band_rows": rows, "dchi2_scaled_from_band": rows < data.N,
+            "build": "reference kernels compiled unmodified from src/functions.cu for sm_103a, "
+                     "launch shapes -X 16 -Y 16 -V 256, cuFFT, the reference's host sequence"}
+
+
+def converge_measure(n_skies):
+    """Time to converge, learned warm start against the plain start, on
+    held-out skies (seeds 900000...) of the 256^2 configuration-0 array:
+    wall time until a line search reaches f <= f* (1 + 1e-4), f* the plain
+    solver's converged objective; the warm time includes the network's
+    forward pass and the start policy."""
+    from gpuvmem_gb300 import warmstart as W
+    path = W.NETWORK_PATH
+    if not os.path.exists(path):
+        return {"unavailable": f"no trained network at {os.path.relpath(path, ROOT)}"}
+    net, meta = W.load_network(path)
+    t0 = time.time()
+    with Clocks() as clk:
+        rows = W.evaluate(net, range(900000, 900000 + n_skies), iterations=300)
+    summ = W.summarize(rows)
+    pol = [r["t_policy"] for r in rows]
+    out = {"skies": n_skies, "seeds": f"900000-{900000 + n_skies - 1} (held out)",
+           "rel": 1e-4, "solver": "CG-FRPRMN (line search on the GPU), chi2 + entropy 0.01",
+           "network": {k: meta[k] for k in ("levels", "base_channels", "train_skies", "epochs")
+                       if k in meta},
+           "policy_ms_median": 1e3 * statistics.median(pol) if pol else None,
+           "seconds": time.time() - t0, "clocks": clk.summary(0)}
+    out.update(summ)
+    return out
 
 
 def max_over_ranks(t, dist, device):
@@ -248,9 +338,19 @@ def run_ours(args):
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     small = data.nvis * 56 <= L2_BYTES
 
-    def step():
+    # the gradient (DChi2 plus the prior gradients) is bracketed by events
+    # inside the timed step: its launches' average duration is the
+    # roofline's
+    evg = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+
+    def step(s=None):
         f, _ = prob.objective(img)
+        if s is not None:
+            evg[s][0].record(stream)
         prob.gradient(img, 1, xi=xi)
+        if s is not None:
+            evg[s][1].record(stream)
         return f
 
     for _ in range(args.warmup):
@@ -267,7 +367,7 @@ def run_ours(args):
             if small:
                 flush.zero_()
             ev[s][0].record(stream)
-            step()
+            step(s)
             ev[s][1].record(stream)
         torch.cuda.synchronize()
     if dist:
@@ -278,11 +378,13 @@ def run_ours(args):
         t = max_over_ranks(t, dist, "cuda")
     value = replica_throughput(world, args.steps, t)
 
-    # DChi2 kernel alone (for the roofline): gv_dchi2 = tcgen05 kernel +
-    # split-K reduce
+    t_grad = sum(a.elapsed_time(b) for a, b in evg) / 1e3 / args.steps
+
+    # DChi2 alone (gv_dchi2 = tcgen05 kernel + split-K reduce), a few
+    # launches after the timed loop
     prob.chi2(img)
     evk = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(max(2, args.steps))]
+           for _ in range(3)]
     for a, b in evk:
         a.record(stream)
         prob.dchi2(img, out=xi)
@@ -325,11 +427,14 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     peaks, src = measured_peaks()
-    peak = peaks["bf16_tflops"] / 3.0
+    # about a second per launch, inside a loop of several seconds: the
+    # sustained (power-capped) peak; the burst figure is reported beside it
+    peak = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]) / 3.0
+    peak_burst = peaks["bf16_tflops"] / 3.0
     V = info.nvis_in_grid
     flops = 4.0 * cfg.n * cfg.n * V
-    achieved = flops / t_dchi2 / 1e12
-    traffic = profile_traffic(V)
+    achieved = flops / t_grad / 1e12
+    traffic = DCHI2_DRAM_BYTES_PER_VIS * V if info.dchi2_engine == 2 else None
     # objective algorithmic bytes: both image planes read once (8 MN), per
     # channel a grid written by the row FFTs and read + written by the column
     # FFTs (16 MN), 20 B per visibility in (u, v, Vo, w) and 8 B of stored
@@ -341,6 +446,17 @@ def run_ours(args):
            "hbm_peak_gbs": peaks["hbm_gbs"], "frac": obj_bytes / t_obj / 1e9 / peaks["hbm_gbs"],
            "note": "8 MN + 16 MN per channel + 28 B per visibility"}
     cpu = cpu_baseline(data, terms, args.cpu_sample_s)
+    refc = None
+    if not args.no_reference_cuda:
+        try:
+            refc = reference_cuda(data, img.cpu().numpy(),
+                                  args.ref_band_rows if cfg.n > 512 else cfg.n)
+            if "evals_per_s" in refc:
+                refc["speedup_value"] = value / refc["evals_per_s"]
+                refc["speedup_e2e"] = e2e / refc["evals_per_s"]
+        except Exception as e:  # the harness is test infrastructure: report, go on
+            refc = {"unavailable": f"{type(e).__name__}: {e}"}
+    conv = converge_measure(args.converge_skies) if args.converge_skies > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
@@ -350,10 +466,17 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(xi.numel() * 4 + 8 * (1 + len(terms)))},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_dchi2_tc (+ split-K reduce)",
-                     "peak_source": f"{src} dense bf16 burst {peaks['bf16_tflops']} TFLOP/s / 3",
-                     "dchi2_ms": 1e3 * t_dchi2, "algorithmic_flop": flops},
+                     "traffic_source": DCHI2_TRAFFIC_SOURCE,
+                     "kernel": "k_dchi2_tc + k_reduce_partials (+ prior gradients): the "
+                               "gradient call, timed inside the timed loop",
+                     "peak_source": f"{src} dense bf16 sustained "
+                                    f"{peaks.get('bf16_tflops_sustained')} TFLOP/s / 3",
+                     "frac_of_burst": achieved / peak_burst,
+                     "gradient_ms": 1e3 * t_grad, "dchi2_alone_ms": 1e3 * t_dchi2,
+                     "algorithmic_flop": flops},
         "objective": obj,
+        "reference_cuda": refc,
+        "converge": conv,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk.summary(local),
         "gpu_launches": int(launches),

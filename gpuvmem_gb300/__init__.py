@@ -371,6 +371,15 @@ class Problem:
         check(lib().gv_optimize(self.h, C.byref(o), _ptr(img), C.byref(rep)))
         return rep
 
+    def mfs_run(self, img, method="CG-FRPRMN", iterations=10, ftol=1e-12, gtol=1e-12, K=100,
+                flags=(0, 1, 2, 3), positivity=True):
+        """MFS::run for a two-image fit without an Order (src/mfs.cu:999-1008):
+        the optimiser runs once per flag, 0 (I_nu0), 1 (alpha), 2 (I_nu0 with
+        the alpha clip below threshold), 3 (alpha), each from the image the
+        previous one left.  Returns the reports."""
+        return [self.optimize(img, method, iterations=iterations, ftol=ftol, gtol=gtol, K=K,
+                              flag=f, positivity=positivity) for f in flags]
+
     def optimize_until(self, img, f_target, method="CG-FRPRMN", iterations=10, ftol=1e-12,
                        gtol=1e-12, K=100, flag=0, positivity=True,
                        priors_from_start=False) -> OptReport:

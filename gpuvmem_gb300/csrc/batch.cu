@@ -138,6 +138,14 @@ gv_status gv_batch_evaluate(gv_batch* b, float* const* d_imgs, float* const* d_x
   auto restore = [&]() {
     for (int i = 0; i < n; i++) gv::problem_of(b->probs[i]).stream = saved[i];
   };
+  // problems run side by side here: no cooperative launches
+  for (int i = 0; i < n; i++) gv::problem_of(b->probs[i]).fused_off++;
+  struct FusedBack {
+    gv_batch* b;
+    ~FusedBack() {
+      for (auto* p : b->probs) gv::problem_of(p).fused_off--;
+    }
+  } fused_back{b};
   if (!b->use_graph) {
     // one problem after another, each on its own stream, one sync at the end
     gv_status s = GV_OK;

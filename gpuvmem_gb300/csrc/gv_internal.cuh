@@ -46,7 +46,9 @@ enum FlagSlot {
   kFlagDegridDone = 4,  // blocks of k_degrid done (the last one finishes chi2)
   kFlagPriorDone = 5,   // blocks of k_prior_values done (the last one sums)
   kFlagOptDone = 6,     // blocks of an optimiser reduction done (the last one sums)
-  kNumFlags = 8
+  kFlagBarCount = 8,    // grid barrier of k_objective_fused: arrivals
+  kFlagBarGen = 9,      // grid barrier of k_objective_fused: generation
+  kNumFlags = 10
 };
 
 struct Channel {
@@ -147,6 +149,10 @@ struct Problem {
   size_t epi_bytes = 0;
   int degrid_threads = 256;      // k_degrid block size
   int degrid_blocks = 0;         // k_degrid blocks per channel cap (0: part_stride)
+  int fused = 1;                 // small images: the objective as one cooperative launch
+                                 // (GV_FUSED=0 at creation turns it off)
+  int fused_off = 0;             // > 0 while callers that run problems concurrently launch
+  int fused_blocks[3] = {0, 0, 0};  // cooperative blocks of k_objective_fused (per image kind)
   void* graphs = nullptr;        // graph cache (graph.cu)
   void* ls_graphs = nullptr;     // device line-search graphs (optim.cu)
   struct LsState* d_ls = nullptr;  // device line-search state

@@ -112,17 +112,14 @@ struct StageParams {
   XtSource xs;       // xs.pcom set: the image is xt = pcom + x xicom (written back)
 };
 
-// Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
-__global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
-                           float* __restrict__ img, const uint8_t* __restrict__ mask,
-                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
-  extern __shared__ float2 sm[];
+// Pass 1 for row i of channel c: stage I_nu * A * fg_scale into buf (shared
+// memory, n float2) and FFT the row with the twiddles tw (shared memory);
+// the row goes to grid.  Every thread of the block takes part.
+__device__ __forceinline__ void row_task(const StageParams& sp, const float* __restrict__ chfreq,
+                                         float* __restrict__ img, const uint8_t* __restrict__ mask,
+                                         const float2* tw, float2* __restrict__ grid, float2* buf,
+                                         int i, int c) {
   const int n = sp.N;
-  float2* buf = sm;
-  float2* tw = sm + n;
-  const int i = blockIdx.x;
-  const int c = blockIdx.y;
-  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
   const float freq = chfreq[c];
   const float nudiv = freq / sp.nu_0;
   const float floor_inu = -1.0f * sp.eta * sp.minpix;
@@ -167,21 +164,32 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
   for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[swz(j, sp.log2n)];
 }
 
-// Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate
-// (src/functions.cu:2483-2518) in the reference's float arithmetic.
-__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __restrict__ rot_u,
-                           const float* __restrict__ rot_v, const float2* __restrict__ tw_g,
-                           float2* __restrict__ grid) {
+// Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
+__global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
+                           float* __restrict__ img, const uint8_t* __restrict__ mask,
+                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
-  const int n = N;
+  const int n = sp.N;
   float2* buf = sm;
-  float2* tw = sm + (size_t)cb * n;
-  const int j0 = blockIdx.x * cb;
-  float2* G = grid + (int64_t)blockIdx.y * MN;
+  float2* tw = sm + n;
   for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
+  row_task(sp, chfreq, img, mask, tw, grid, buf, blockIdx.x, blockIdx.y);
+}
+
+// Pass 2 for columns j0 .. j0 + cb - 1 of grid G: column FFTs in buf
+// (shared memory, cb * n float2), then phase_rotate (src/functions.cu:
+// 2483-2518) in the reference's float arithmetic.  Load: how the grid is
+// read (plain loads, or L2 loads when the grid was written earlier in the
+// same kernel by other blocks).
+template <bool kL2Loads>
+__device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* __restrict__ rot_u,
+                                         const float* __restrict__ rot_v, const float2* tw,
+                                         float2* __restrict__ G, float2* buf, int j0) {
+  const int n = N;
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
-    buf[cc * n + swz(bitrev(r, log2n), log2n)] = G[(int64_t)n * r + j0 + cc];
+    const float2* src = G + (int64_t)n * r + j0 + cc;
+    buf[cc * n + swz(bitrev(r, log2n), log2n)] = kL2Loads ? __ldcg(src) : *src;
   }
   __syncthreads();
   smem_fft(buf, log2n, cb, tw);
@@ -197,6 +205,19 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __
     sincospif(phase, &s, &co);
     G[(int64_t)n * r + j] = cmul(buf[cc * n + swz(r, log2n)], make_float2(co, s));
   }
+}
+
+// Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate.
+__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __restrict__ rot_u,
+                           const float* __restrict__ rot_v, const float2* __restrict__ tw_g,
+                           float2* __restrict__ grid) {
+  extern __shared__ float2 sm[];
+  const int n = N;
+  float2* buf = sm;
+  float2* tw = sm + (size_t)cb * n;
+  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
+  col_task<false>(N, log2n, cb, rot_u, rot_v, tw, grid + (int64_t)blockIdx.y * MN, buf,
+                  blockIdx.x * cb);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -239,33 +260,52 @@ __device__ void finish_chi2(int C, int nb, const double* part, int part_stride,
   if (threadIdx.x == 0) *out = 0.5 * tot;
 }
 
-// Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
-// block to finish adds the partials into the chi2 scalar.
-__global__ void __launch_bounds__(256) k_degrid(
-    int N, int64_t MN, const ChanRange* __restrict__ ranges,
-    const float4* __restrict__ deg, const float2* __restrict__ vo,
-    const float2* __restrict__ grid, float2* __restrict__ cvr, int store,
-    double* __restrict__ part, int part_stride, uint32_t* __restrict__ cmax,
-    uint32_t* __restrict__ done, const int64_t* __restrict__ nvis, int normalize,
-    double* __restrict__ chi2_out, double* __restrict__ term_out, uint32_t zero_terms,
-    double* __restrict__ term_slots) {
-  const int c = blockIdx.y;
+// Arguments of pass 3 (and of its finish).
+struct DegridArgs {
+  int N;
+  int64_t MN;
+  const ChanRange* __restrict__ ranges;
+  const float4* __restrict__ deg;
+  const float2* __restrict__ vo;
+  const float2* __restrict__ grid;
+  float2* __restrict__ cvr;
+  int store;
+  double* __restrict__ part;
+  int part_stride;
+  uint32_t* __restrict__ cmax;
+  uint32_t* __restrict__ done;
+  const int64_t* __restrict__ nvis;
+  int normalize;
+  double* __restrict__ chi2_out;
+  double* __restrict__ term_out;
+  uint32_t zero_terms;
+  double* __restrict__ term_slots;
+};
+
+// Pass 3 for block b of nb of channel c: vis_mod + residual + chi2Vector
+// over the block's share of the cell-sorted visibilities and the block's
+// FP64 partial; the last of the nb * C blocks to finish adds the partials
+// into the chi2 scalar.  kL2Loads: read the grid from L2 (written earlier in
+// the same kernel by other blocks).
+template <bool kL2Loads>
+__device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
   float mx = 0.0f;
-  const ChanRange rg = ranges[c];
-  const float2* __restrict__ G = grid + (int64_t)c * MN;
+  const ChanRange rg = a.ranges[c];
+  const float2* __restrict__ G = a.grid + (int64_t)c * a.MN;
+  const int N = a.N;
   const int nm1 = N - 1;
   CompSum acc;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const float4 d = __ldcs(deg + rg.off + k);
-    const float2 o = __ldcs(vo + rg.off + k);
+  for (int64_t k = b * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
+       k += (int64_t)nb * blockDim.x) {
+    const float4 d = __ldcs(a.deg + rg.off + k);
+    const float2 o = __ldcs(a.vo + rg.off + k);
     const uint32_t cell = __float_as_uint(d.x);
     const int i1 = cell & 0xffff, j1 = cell >> 16;
     const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
-    const float2 v11 = __ldg(G + (int64_t)N * j1 + i1);
-    const float2 v12 = __ldg(G + (int64_t)N * j2 + i1);
-    const float2 v21 = __ldg(G + (int64_t)N * j1 + i2);
-    const float2 v22 = __ldg(G + (int64_t)N * j2 + i2);
+    const float2 v11 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i1) : __ldg(G + (int64_t)N * j1 + i1);
+    const float2 v12 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i1) : __ldg(G + (int64_t)N * j2 + i1);
+    const float2 v21 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i2) : __ldg(G + (int64_t)N * j1 + i2);
+    const float2 v22 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i2) : __ldg(G + (int64_t)N * j2 + i2);
     const float du = d.y, dv = d.z;
     const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
     const float w21 = du * (1.0f - dv), w22 = du * dv;
@@ -273,28 +313,34 @@ __global__ void __launch_bounds__(256) k_degrid(
     const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
     const float rr = o.x - mr, ri = o.y - mi;
     acc.add(d.w * (rr * rr + ri * ri));
-    if (store) {
+    if (a.store) {
       const float2 cv = make_float2(d.w * rr, d.w * ri);
-      __stcs(cvr + rg.off + k, cv);
+      __stcs(a.cvr + rg.off + k, cv);
       mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
     }
   }
-  if (store) {
+  if (a.store) {
     for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, s));
-    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(cmax, __float_as_uint(mx));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(a.cmax, __float_as_uint(mx));
   }
   const double bsum = block_sum(acc.value());
-  if (threadIdx.x == 0) part[(int64_t)c * part_stride + blockIdx.x] = bsum;
-  if (last_block_done(done, gridDim.x * gridDim.y)) {
-    finish_chi2(gridDim.y, gridDim.x, part, part_stride, nvis, normalize, chi2_out);
+  if (threadIdx.x == 0) a.part[(int64_t)c * a.part_stride + b] = bsum;
+  if (last_block_done(a.done, nb * C)) {
+    finish_chi2(C, nb, a.part, a.part_stride, a.nvis, a.normalize, a.chi2_out);
     if (threadIdx.x == 0) {
       // ObjectiveFunction's per-term values: chi2's own slot, and 0 for the
       // priors the iteration gating leaves out
-      if (term_out) *term_out = *chi2_out;
+      if (a.term_out) *a.term_out = *a.chi2_out;
       for (int t = 0; t < 32; t++)
-        if (zero_terms & (1u << t)) term_slots[t] = 0.0;
+        if (a.zero_terms & (1u << t)) a.term_slots[t] = 0.0;
     }
   }
+}
+
+// Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
+// block to finish adds the partials into the chi2 scalar.
+__global__ void __launch_bounds__(256) k_degrid(DegridArgs a) {
+  degrid_task<false>(a, blockIdx.x, gridDim.x, blockIdx.y, gridDim.y);
 }
 
 // ---- priors ---------------------------------------------------------------
@@ -438,6 +484,24 @@ struct XtImage {
   }
 };
 
+// ClipImage: the image as clip2IWNoise leaves it, formed per pixel (the
+// clip is idempotent, so the value is the same whether or not the staging
+// has written the clipped pixel back yet); read through L2, as the image is
+// written in the same kernel.
+struct ClipImage {
+  const float* p;
+  const uint8_t* mask;
+  int64_t MN;
+  ClipRule cr;
+  int plane;
+  __device__ void bind() {}
+  __device__ __forceinline__ float operator[](int64_t q) const {
+    float i0 = __ldcg(p + q), al = __ldcg(p + MN + q);
+    clip_pixel(mask[q], cr, i0, al);
+    return plane ? al : i0;
+  }
+};
+
 template <class Img>
 struct PriorSet {
   int n;
@@ -447,33 +511,40 @@ struct PriorSet {
   double* out[kMaxTerms];   // the term's value
 };
 
-// Values of n prior terms (blockIdx.y = term): per-block partials, and the
-// last block to finish sums each term's partials in a fixed order.
+// Values of n prior terms, block b of nb of term t: the block's partial, and
+// the last of the nb * n blocks to finish sums each term's partials in a
+// fixed order.
 template <class Img>
-__global__ void __launch_bounds__(256) k_prior_values(PriorSet<Img> ps,
-                                                      const uint8_t* __restrict__ mask,
-                                                      uint32_t* __restrict__ done) {
-  const int t = blockIdx.y;
-  const PriorParams pp = ps.pp[t];
+__device__ __forceinline__ void prior_task(const PriorSet<Img>& ps, const uint8_t* __restrict__ mask,
+                                           uint32_t* __restrict__ done, int b, int nb, int t) {
+  const PriorParams& pp = ps.pp[t];
   Img I = ps.img[t];
   I.bind();
   CompSum acc;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
-       q += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t q = b * (int64_t)blockDim.x + threadIdx.x; q < pp.MN;
+       q += (int64_t)nb * blockDim.x) {
     if (!(mask[q] & kMaskIn)) continue;
     const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
     acc.add(prior_pixel(pp, I, i, j));
   }
   const double bsum = block_sum(acc.value());
-  if (threadIdx.x == 0) ps.part[t][blockIdx.x] = bsum;
-  if (last_block_done(done, gridDim.x * gridDim.y)) {
+  if (threadIdx.x == 0) ps.part[t][b] = bsum;
+  if (last_block_done(done, nb * ps.n)) {
     for (int u = 0; u < ps.n; u++) {
       double v = 0.0;
-      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(ps.part[u] + b);
+      for (int k = threadIdx.x; k < nb; k += blockDim.x) v += __ldcg(ps.part[u] + k);
       v = block_sum(v);
       if (threadIdx.x == 0) *ps.out[u] = v;
     }
   }
+}
+
+// Values of n prior terms (blockIdx.y = term).
+template <class Img>
+__global__ void __launch_bounds__(256) k_prior_values(PriorSet<Img> ps,
+                                                      const uint8_t* __restrict__ mask,
+                                                      uint32_t* __restrict__ done) {
+  prior_task(ps, mask, done, blockIdx.x, gridDim.x, blockIdx.y);
 }
 
 __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float* __restrict__ I,
@@ -486,6 +557,120 @@ __global__ void __launch_bounds__(256) k_prior_grad(PriorParams pp, const float*
     const float g = prior_grad_pixel(pp, I, i, j) * pp.lambda;
     dphi[q] += g;  // AddToDPhi, src/functions.cu:3890
   }
+}
+
+// ---- small images: the whole objective in one cooperative launch --------
+//
+// Below 512 x 512 an evaluation is a few microseconds of work spread over
+// four dependent launches, and the launches set its time.  k_objective_fused
+// runs the same passes in one cooperative launch (every block resident):
+//   A  row tasks (pass 1) and prior-value tasks, then a grid barrier;
+//   B  column tasks (pass 2), then a grid barrier;
+//   C  degridding tasks (pass 3); the last task to finish sums chi2.
+// Every task is the corresponding kernel's block, with the same block size
+// and the same partial-sum slots, so the results are bit-identical to the
+// four launches.  Data written in the kernel is read back through L2
+// (ld.global.cg), never through a block's L1.
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier of a cooperative launch.  bar[0] counts arrivals, bar[1]
+// is the generation: the last block to arrive resets the count and advances
+// the generation.  The wait is bounded (1 s): on time-out the error word
+// gets bit 16 and false is returned in every thread of the block (the
+// caller leaves the kernel).
+__device__ bool grid_barrier(uint32_t* bar, uint32_t* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t gen = ld_acquire_gpu(bar + 1);
+    __threadfence();
+    const uint32_t prev = atomicAdd(bar, 1u);
+    int good = 1;
+    if (prev == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const uint64_t t0 = global_ns();
+      while (ld_acquire_gpu(bar + 1) == gen) {
+        __nanosleep(32);
+        if (global_ns() - t0 > 1000000000ull) {
+          atomicOr(err, 16u);
+          good = 0;
+          break;
+        }
+      }
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <class Img>
+struct FusedArgs {
+  StageParams sp;
+  const float* chfreq;
+  float* img;
+  const uint8_t* mask;
+  const float2* tw;
+  const float* rot_u;
+  const float* rot_v;
+  int C;
+  int cb;          // columns per column task
+  int nb_deg;      // degridding tasks per channel (k_degrid's blocks)
+  int nb_prior;    // prior tasks per term (k_prior_values' blocks)
+  DegridArgs da;
+  PriorSet<Img> ps;
+  uint32_t* prior_done;
+  uint32_t* bar;   // [2] grid barrier
+  uint32_t* err;
+};
+
+template <class Img>
+__global__ void __launch_bounds__(256) k_objective_fused(FusedArgs<Img> f) {
+  extern __shared__ float2 sm[];
+  const int n = f.sp.N;
+  float2* buf = sm;              // n * cb values
+  float2* tw = sm + n * f.cb;    // n - 1 twiddles
+  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = f.tw[k];
+  __syncthreads();
+  float2* grid = const_cast<float2*>(f.da.grid);
+  // A: rows of every channel, then the prior-value tasks
+  const int nrow = n * f.C;
+  const int ntask_a = nrow + f.nb_prior * f.ps.n;
+  for (int t = blockIdx.x; t < ntask_a; t += gridDim.x) {
+    if (t < nrow) {
+      row_task(f.sp, f.chfreq, f.img, f.mask, tw, grid, buf, t % n, t / n);
+    } else {
+      const int u = t - nrow;
+      prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
+    }
+    __syncthreads();
+  }
+  if (!grid_barrier(f.bar, f.err)) return;
+  // B: columns
+  const int ncg = n / f.cb;
+  for (int t = blockIdx.x; t < ncg * f.C; t += gridDim.x) {
+    col_task<true>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, tw, grid + (int64_t)(t / ncg) * f.sp.MN,
+                   buf, (t % ncg) * f.cb);
+    __syncthreads();
+  }
+  if (!grid_barrier(f.bar, f.err)) return;
+  // C: degridding and chi2
+  for (int t = blockIdx.x; t < f.nb_deg * f.C; t += gridDim.x)
+    degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C);
 }
 
 }  // namespace
@@ -502,11 +687,8 @@ static int cols_per_block(int n, int channels, int num_sms) {
   return cb;
 }
 
-// Model grids of all channels for image d_img (clip written back when
-// write_clip).
-gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_clip,
-                             const XtSource* xs = nullptr) {
-  const int n = P.N, C = (int)P.chans.size();
+static StageParams stage_params(const Problem& P, int flag_opt, int write_clip,
+                                const XtSource* xs) {
   StageParams sp;
   sp.M = P.M;
   sp.N = P.N;
@@ -531,6 +713,15 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   sp.beam_x = P.d_beam_x;
   sp.beam_y = P.d_beam_y;
   sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0f, 0};
+  return sp;
+}
+
+// Model grids of all channels for image d_img (clip written back when
+// write_clip).
+gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_clip,
+                             const XtSource* xs = nullptr) {
+  const int n = P.N, C = (int)P.chans.size();
+  const StageParams sp = stage_params(P, flag_opt, write_clip, xs);
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
   const size_t sm1 = sizeof(float2) * (2 * n - 1);
   if (sm1 > 48 * 1024)
@@ -548,25 +739,121 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   return GV_OK;
 }
 
-gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
-                      const XtSource* xs, double* term_out, uint32_t zero_terms) {
-  gv_status s = model_grids_launch(P, d_img, flag_opt, 1, xs);
-  if (s != GV_OK) return s;
-  const int C = (int)P.chans.size();
+// k_degrid's blocks per channel
+static int degrid_blocks(const Problem& P) {
   int64_t maxg = 1;
   for (auto& ch : P.chans) maxg = std::max<int64_t>(maxg, ch.ngrid);
   const int th = P.degrid_threads;
   const int cap = P.degrid_blocks > 0 ? std::min(P.degrid_blocks, P.part_stride) : P.part_stride;
-  int nb = (int)std::min<int64_t>((maxg + th - 1) / th, cap);
-  if (nb < 1) nb = 1;
+  const int nb = (int)std::min<int64_t>((maxg + th - 1) / th, cap);
+  return nb < 1 ? 1 : nb;
+}
+
+static DegridArgs degrid_args(Problem& P, bool store_res, double* term_out, uint32_t zero_terms) {
   const int64_t MN = (int64_t)P.M * P.N;
+  return DegridArgs{P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid, P.d_cvr,
+                    store_res ? 1 : 0, P.d_part, P.part_stride, P.d_flags + kFlagCvrMax,
+                    P.d_flags + kFlagDegridDone, P.d_chnvis, P.normalize,
+                    P.d_scal + kSlotChi2, term_out, zero_terms, P.d_scal + kSlotTerm0};
+}
+
+static int prior_blocks(const Problem& P) {
+  const int64_t MN = (int64_t)P.M * P.N;
+  return (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
+}
+
+// Whether the objective of P runs as k_objective_fused: images up to
+// 512 x 512 (where launches dominate), k_degrid's default block size (the
+// fused tasks reproduce its 256-thread blocks), and no caller running
+// several problems at once (cooperative launches must not share the GPU
+// with each other).
+static bool fused_ok(const Problem& P) {
+  return P.fused && P.fused_off == 0 && P.N <= 512 && P.degrid_threads == 256;
+}
+
+template <class Img>
+struct ImgKind;
+template <>
+struct ImgKind<PlainImage> {
+  static constexpr int k = 0;
+};
+template <>
+struct ImgKind<ClipImage> {
+  static constexpr int k = 1;
+};
+template <>
+struct ImgKind<XtImage> {
+  static constexpr int k = 2;
+};
+
+// The objective's passes (and the prior values of ps) in one cooperative
+// launch; same outputs as model_grids_launch + k_degrid (+ k_prior_values).
+template <class Img>
+static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                              const XtSource* xs, double* term_out, uint32_t zero_terms,
+                              const PriorSet<Img>& ps) {
+  const int n = P.N, C = (int)P.chans.size();
+  FusedArgs<Img> f{};
+  f.sp = stage_params(P, flag_opt, 1, xs);
+  f.chfreq = P.d_chfreq;
+  f.img = d_img;
+  f.mask = P.d_mask;
+  f.tw = P.d_twiddle;
+  f.rot_u = P.d_rot_u;
+  f.rot_v = P.d_rot_v;
+  f.C = C;
+  f.cb = 1;
+  f.nb_deg = degrid_blocks(P);
+  f.nb_prior = prior_blocks(P);
+  f.da = degrid_args(P, store_res, term_out, zero_terms);
+  f.ps = ps;
+  f.prior_done = P.d_flags + kFlagPriorDone;
+  f.bar = P.d_flags + kFlagBarCount;
+  f.err = P.d_flags + kFlagErr;
+  const size_t smem = sizeof(float2) * (size_t)(n - 1 + n * f.cb);
+  int& blocks = P.fused_blocks[ImgKind<Img>::k];
+  if (blocks == 0) {
+    // every block must be resident at once: at most the occupancy bound,
+    // two blocks per SM at most, and no more than the largest pass has tasks
+    int occ = 0;
+    GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_objective_fused<Img>, 256,
+                                                          smem));
+    if (occ < 1) {
+      set_error("k_objective_fused does not fit on an SM");
+      return GV_ERR_UNSUPPORTED;
+    }
+    const int tasks = std::max(n * C + f.nb_prior * kMaxTerms, f.nb_deg * C);
+    blocks = std::max(1, std::min(P.num_sms * std::min(occ, 2), tasks));
+  }
   if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
-  k_degrid<<<dim3(nb, C), th, 0, P.stream>>>(P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid,
-                                              P.d_cvr, store_res ? 1 : 0, P.d_part, P.part_stride,
-                                              P.d_flags + kFlagCvrMax,
-                                              P.d_flags + kFlagDegridDone, P.d_chnvis,
-                                              P.normalize, P.d_scal + kSlotChi2, term_out,
-                                              zero_terms, P.d_scal + kSlotTerm0);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = P.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GV_CUDA(cudaLaunchKernelEx(&cfg, k_objective_fused<Img>, f));
+  GV_LAUNCH("k_objective_fused");
+  return GV_OK;
+}
+
+gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                      const XtSource* xs, double* term_out, uint32_t zero_terms) {
+  if (fused_ok(P)) {
+    PriorSet<PlainImage> none{};
+    return fused_launch(P, d_img, flag_opt, store_res, xs, term_out, zero_terms, none);
+  }
+  gv_status s = model_grids_launch(P, d_img, flag_opt, 1, xs);
+  if (s != GV_OK) return s;
+  const int C = (int)P.chans.size();
+  const int nb = degrid_blocks(P);
+  if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
+  const DegridArgs da = degrid_args(P, store_res, term_out, zero_terms);
+  k_degrid<<<dim3(nb, C), P.degrid_threads, 0, P.stream>>>(da);
   GV_LAUNCH("k_degrid");
   return GV_OK;
 }
@@ -583,11 +870,6 @@ static PriorParams prior_params(const Problem& P, const Term& t) {
   pp.eps_b = t.epsilon_b;
   pp.prior = t.d_prior;
   return pp;
-}
-
-static int prior_blocks(const Problem& P) {
-  const int64_t MN = (int64_t)P.M * P.N;
-  return (int)std::min<int64_t>((MN + 255) / 256, P.part_stride);
 }
 
 static double* prior_part(Problem& P, int t) {
@@ -647,6 +929,28 @@ gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_re
   for (size_t t = 0; t < P.terms.size(); t++) {
     if (P.terms[t].kind == GV_FI_CHI2) has_chi2 = true;
     else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) zero |= 1u << t;
+  }
+  if (fused_ok(P) && !P.terms.empty() && P.terms[0].kind == GV_FI_CHI2) {
+    // Chi2 first, so the priors see the clipped image: every active prior
+    // rides in the same cooperative launch
+    PriorSet<ClipImage> ps{};
+    const int64_t MN = (int64_t)P.M * P.N;
+    const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
+                      flag_opt};
+    bool fits = true;
+    for (size_t t = 1; t < P.terms.size(); t++) {
+      const Term& tm = P.terms[t];
+      if (tm.kind == GV_FI_CHI2) fits = false;
+      if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
+      const int k = ps.n++;
+      ps.pp[k] = prior_params(P, tm);
+      ps.img[k] = ClipImage{d_img, P.d_mask, MN, cr, tm.image_index};
+      ps.part[k] = prior_part(P, (int)t);
+      ps.out[k] = P.d_scal + kSlotTerm0 + t;
+    }
+    if (fits)
+      return fused_launch(P, d_img, flag_opt, store_res, nullptr, P.d_scal + kSlotTerm0, zero,
+                          ps);
   }
   int run[kMaxTerms], slots[kMaxTerms], nrun = 0;
   auto flush = [&]() -> gv_status {
@@ -708,6 +1012,8 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
     ps.part[k] = prior_part(P, (int)t);
     ps.out[k] = P.d_scal + kSlotTerm0 + t;
   }
+  if (fused_ok(P))
+    return fused_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero, ps);
   if (ps.n > 0) {
     GV_CUDA(cudaEventRecord(fork, P.stream));
     GV_CUDA(cudaStreamWaitEvent(side, fork, 0));
@@ -728,6 +1034,8 @@ gv_status check_device_error(Problem& P) {
   GV_CUDA(cudaStreamSynchronize(P.stream));
   if (e != 0) {
     GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagErr, 0, sizeof(uint32_t), P.stream));
+    // a grid barrier that timed out leaves its arrival count behind
+    GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagBarCount, 0, sizeof(uint32_t), P.stream));
     set_error("a kernel gave up on a bounded wait (device error word " + std::to_string(e) + ")");
     return GV_ERR_DEVICE;
   }

@@ -609,6 +609,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     const char* g = std::getenv("GV_GRAPHS");
     P.use_graphs = (g && g[0] == '0') ? 0 : 1;
   }
+  if (const char* e = std::getenv("GV_FUSED")) P.fused = std::atoi(e) != 0 ? 1 : 0;
   P.part_stride = 4 * P.num_sms;
   const int nslots = C + kMaxTerms + 8;
   GV_CUDA(cudaMalloc(&P.d_part, sizeof(double) * (size_t)P.part_stride * nslots));

@@ -26,6 +26,7 @@ from __future__ import annotations
 import argparse
 import dataclasses
 import json
+import os
 import time
 from typing import List, Optional, Sequence
 
@@ -35,6 +36,9 @@ from . import Problem, synth, term
 from .unet import UNet
 
 CONFIG4 = dataclasses.replace(synth.CONFIG0, name="learned-256", array_seed=synth.CONFIG0.seed)
+# the trained network shipped with the package (written by `main --save`)
+NETWORK_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                            "warmstart_unet.npz")
 TERMS = (("Chi2", 1.0), ("Entropy", 0.01))
 
 
@@ -119,6 +123,77 @@ def train(X, Y, epochs=80, batch=8, lr=1e-3, lr_min=1e-5, base_channels=16, leve
         if log:
             log(f"epoch {ep + 1}/{epochs} loss {hist[-1]:.4e}")
     return net, hist
+
+
+def param_layout(in_channels: int, base_channels: int, levels: int):
+    """gv_unet's parameter vector, layer by layer: (weight offset, weight
+    count, bias offset, bias count).  Encoder: two 3x3 convolutions per
+    level (channels base * 2^l); decoder: two 3x3 convolutions per level on
+    the upsampled deeper level concatenated with the skip connection; a
+    final 1x1 convolution to one channel.  Each layer stores its weights
+    [out][in][ky][kx], then its biases."""
+    ch = [base_channels << l for l in range(levels)]
+    layers = []
+    for l in range(levels):
+        layers.append((in_channels if l == 0 else ch[l - 1], ch[l], 3))
+        layers.append((ch[l], ch[l], 3))
+    for l in range(levels - 2, -1, -1):
+        layers.append((ch[l + 1] + ch[l], ch[l], 3))
+        layers.append((ch[l], ch[l], 3))
+    layers.append((ch[0], 1, 1))
+    out, off = [], 0
+    for ci, co, ks in layers:
+        nw = co * ci * ks * ks
+        out.append((off, nw, off + nw, co))
+        off += nw + co
+    return out, off
+
+
+def _bf16_bits(x):
+    """float32 -> bfloat16 bit patterns, round to nearest even (the rounding
+    the convolution kernels apply to their operands)."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) >> 16
+    return b.astype(np.uint16)
+
+
+def save_network(net: UNet, path: str, meta: dict):
+    """Writes the network's parameters: convolution weights as bfloat16 (the
+    kernels round weights to BF16 before every product, so nothing is lost
+    for the forward pass), biases as float32, and `meta` (shape and training
+    record) as JSON."""
+    lay, n = param_layout(net.desc.in_channels, net.desc.base_channels, net.desc.levels)
+    assert n == net.nparams, (n, net.nparams)
+    theta = net.params().cpu().numpy()
+    w = np.concatenate([theta[o:o + k] for o, k, _, _ in lay])
+    b = np.concatenate([theta[o:o + k] for _, _, o, k in lay])
+    m = dict(meta, height=net.H, in_channels=net.desc.in_channels,
+             base_channels=net.desc.base_channels, levels=net.desc.levels)
+    np.savez_compressed(path, weights_bf16=_bf16_bits(w), biases=b.astype(np.float32),
+                        meta=np.frombuffer(json.dumps(m).encode(), dtype=np.uint8))
+
+
+def load_network(path: str, max_batch: int = 1):
+    """(UNet with the saved parameters, meta dict)."""
+    import torch
+    z = np.load(path)
+    meta = json.loads(bytes(z["meta"]).decode())
+    net = UNet(meta["height"], in_channels=meta["in_channels"],
+               base_channels=meta["base_channels"], levels=meta["levels"], max_batch=max_batch,
+               seed=0)
+    lay, n = param_layout(meta["in_channels"], meta["base_channels"], meta["levels"])
+    assert n == net.nparams, (n, net.nparams)
+    w = (z["weights_bf16"].astype(np.uint32) << 16).view(np.float32)
+    b = z["biases"].astype(np.float32)
+    theta = np.empty(n, np.float32)
+    wi = bi = 0
+    for wo, wk, bo, bk in lay:
+        theta[wo:wo + wk] = w[wi:wi + wk]
+        theta[bo:bo + bk] = b[bi:bi + bk]
+        wi += wk
+        bi += bk
+    net.set_params(torch.from_numpy(theta).cuda())
+    return net, meta
 
 
 def warm_image(sky: Sky, net: UNet):
@@ -231,6 +306,15 @@ def summarize(rows: List[dict]) -> dict:
 
 
 def main(argv: Optional[Sequence[str]] = None):
+    """Trains and evaluates the warm start.  The network shipped in
+    gpuvmem_gb300/data/warmstart_unet.npz was made by
+
+        python -m gpuvmem_gb300.warmstart --train 2000 --eval 200 --epochs 40 \
+            --shapes 4x32,5x16 --save gpurun_out/unet_{shape}.npz --out gpurun_out/ws.json
+
+    (pairs from the plain solver on seeds 1000-2999, the held-out skies are
+    seeds 900000-900199), keeping the shape with the larger summed-time
+    speed-up."""
     ap = argparse.ArgumentParser(description="train and evaluate the learned warm start")
     ap.add_argument("--train", type=int, default=512)
     ap.add_argument("--eval", type=int, default=32)
@@ -240,35 +324,54 @@ def main(argv: Optional[Sequence[str]] = None):
     ap.add_argument("--lr-min", type=float, default=1e-5)
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--base-channels", type=int, default=16)
+    ap.add_argument("--shapes", default=None,
+                    help="comma-separated LEVELSxBASE shapes trained on the same pairs "
+                         "(overrides --levels / --base-channels)")
     ap.add_argument("--pair-iterations", type=int, default=150)
     ap.add_argument("--eval-iterations", type=int, default=300)
     ap.add_argument("--out", default=None, help="write the summary JSON here")
+    ap.add_argument("--save", default=None,
+                    help="write the trained network here (.npz; {shape} is replaced by "
+                         "LEVELSxBASE)")
+    ap.add_argument("--train-seed0", type=int, default=1000)
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)  # noqa: E731
+    shapes = ([tuple(int(v) for v in sh.split("x")) for sh in a.shapes.split(",")]
+              if a.shapes else [(a.levels, a.base_channels)])
     t0 = time.time()
-    X, Y, _ = make_pairs(range(1000, 1000 + a.train), a.pair_iterations, log=log)
+    X, Y, _ = make_pairs(range(a.train_seed0, a.train_seed0 + a.train), a.pair_iterations,
+                         log=log)
     t_pairs = time.time() - t0
     log(f"targets: mean {float(Y.mean()):.3e} max {float(Y.max()):.3e} "
         f"mean square {float((Y * Y).mean()):.3e}")
-    net, hist = train(X, Y, a.epochs, a.batch, a.lr, a.lr_min, a.base_channels, a.levels,
-                      log=log)
     Xv, Yv, _ = make_pairs(range(900000, 900000 + min(a.eval, 16)), a.pair_iterations)
-    val = float(np.mean([((net.forward(Xv[i:i + 1]) - Yv[i:i + 1]) ** 2).mean().item()
-                         for i in range(Xv.shape[0])]))
-    log(f"held-out mse {val:.4e} (target mean square {float((Yv * Yv).mean()):.4e})")
-    del Xv, Yv
-    t_train = time.time() - t0 - t_pairs
-    rows = evaluate(net, range(900000, 900000 + a.eval), a.eval_iterations, log=log)
-    summ = summarize(rows)
-    summ.update({"train_skies": a.train, "epochs": a.epochs, "levels": a.levels,
-                 "base_channels": a.base_channels, "final_train_loss": hist[-1],
-                 "heldout_mse": val,
-                 "pair_generation_s": t_pairs, "training_s": t_train})
-    print(json.dumps(summ), flush=True)
+    results = {}
+    for levels, base in shapes:
+        tag = f"{levels}x{base}"
+        t1 = time.time()
+        net, hist = train(X, Y, a.epochs, a.batch, a.lr, a.lr_min, base, levels, log=log)
+        t_train = time.time() - t1
+        val = float(np.mean([((net.forward(Xv[i:i + 1]) - Yv[i:i + 1]) ** 2).mean().item()
+                             for i in range(Xv.shape[0])]))
+        log(f"{tag}: held-out mse {val:.4e} (target mean square {float((Yv * Yv).mean()):.4e})")
+        if a.save:
+            save_network(net, a.save.replace("{shape}", tag),
+                         {"train_skies": a.train, "train_seed0": a.train_seed0,
+                          "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "lr_min": a.lr_min,
+                          "pair_iterations": a.pair_iterations, "final_train_loss": hist[-1],
+                          "heldout_mse": val})
+        rows = evaluate(net, range(900000, 900000 + a.eval), a.eval_iterations, log=log)
+        summ = summarize(rows)
+        summ.update({"train_skies": a.train, "epochs": a.epochs, "levels": levels,
+                     "base_channels": base, "final_train_loss": hist[-1], "heldout_mse": val,
+                     "pair_generation_s": t_pairs, "training_s": t_train})
+        print(json.dumps(summ), flush=True)
+        results[tag] = {"summary": summ, "rows": rows, "loss_history": hist}
+        del net
     if a.out:
         with open(a.out, "w") as f:
-            json.dump({"summary": summ, "rows": rows, "loss_history": hist}, f, indent=1)
-    return summ
+            json.dump(results, f, indent=1)
+    return results
 
 
 if __name__ == "__main__":

@@ -158,7 +158,7 @@ def test_plain256_vs_reference_kernels(plain256):
             v_orc = orc.prior_value(ti, img_orc)
             v_ours = prob.prior_value(ti, d)
             gp = prob.prior_gradient(ti, d).cpu().numpy()[0]
-            gp_orc = lam * orc.prior_grad(ti, img_orc)
+            gp_orc = orc.prior_grad(ti, img_orc)  # lambda * gradient
             e[f"prior {kind} value ours-ref"] = abs(v_ours - v_ref) / abs(v_ref)
             e[f"prior {kind} value ours-oracle"] = abs(v_ours - v_orc) / abs(v_orc)
             e[f"prior {kind} grad ours-ref"] = np.abs(gp - gr_ref).max() / np.abs(gp_orc).max()
@@ -170,6 +170,7 @@ def test_plain256_vs_reference_kernels(plain256):
         for kind in (1, 2):
             assert e[f"prior {kind} value ours-ref"] <= CHI2_RTOL
             assert e[f"prior {kind} grad ours-ref"] <= GRAD_TOL
+            assert e[f"prior {kind} grad ours-oracle"] <= GRAD_TOL
     finally:
         ref.close()
 
@@ -265,20 +266,25 @@ def test_plain2048_gradient_sampled(plain2048):
             i0 = min(max(0, row // 16 * 16), data.N - 16)
             band = ref.dchi2_band(img_ref, i0, 16)[0]
             ours_band = g_ours[0, i0:i0 + 16]
-            e_band = np.abs(ours_band - band).max() / scale
+            diff = np.abs(ours_band - band).reshape(-1)
+            e_band = diff.max() / scale
+            # the oracle decides at the 32 pixels where ours and the
+            # reference disagree most, plus 32 random ones of the band
             inband = np.arange(i0 * data.N, (i0 + 16) * data.N)
-            bp = sample_pixels(orc.mask.reshape(-1)[inband], rng, 64) + i0 * data.N
-            bp = np.unique(np.concatenate([bp, [qmax]]))
+            worst = np.argsort(diff)[-32:] + i0 * data.N
+            bp = sample_pixels(orc.mask.reshape(-1)[inband], rng, 32) + i0 * data.N
+            bp = np.unique(np.concatenate([bp, worst, [qmax]])).astype(np.int64)
             g_orc_b, _ = oracle_grad_pixels(orc, data, img_c, bp, 0)
             e_ref_orc = np.abs(band.reshape(-1)[bp - i0 * data.N] - g_orc_b).max() / scale
             e_ours_orc_b = np.abs(g_ours[0].reshape(-1)[bp] - g_orc_b).max() / scale
-            msg += (f"; rows {i0}-{i0 + 15}: ours-ref {e_band:.2e}, ref-oracle {e_ref_orc:.2e}, "
-                    f"ours-oracle {e_ours_orc_b:.2e} (at {bp.size} pixels)")
+            msg += (f"; rows {i0}-{i0 + 15} ({band.size} pixels): ours-ref max {e_band:.2e}; at "
+                    f"{bp.size} pixels incl. the 32 largest disagreements: ref-oracle "
+                    f"{e_ref_orc:.2e}, ours-oracle {e_ours_orc_b:.2e}")
             # the reference's FP32 running sum over 4.41M visibilities per
-            # channel is itself off the FP64 value: ours may differ from it
-            # by no more than its own error plus the gate
-            assert e_band <= e_ref_orc + GRAD_TOL
+            # channel is itself off the FP64 value by more than the gate:
+            # where the two disagree, ours is the one within the gate
             assert e_ours_orc_b <= GRAD_TOL
+            assert e_band <= e_ref_orc + GRAD_TOL
         finally:
             ref.close()
     print(msg)
