@@ -113,7 +113,7 @@ struct Problem {
   uint8_t* d_mask = nullptr;     // [MN]
   float* d_rho = nullptr;        // [MN] z - 1 + r^2/2 per pixel
   float2* d_grid = nullptr;      // [C][MN] model grids
-  float2* d_twiddle = nullptr;   // [n-1] e^{+2 pi i k/n}, stage-major (objective.cu smem_fft)
+  float2* d_twiddle = nullptr;   // [n] e^{+2 pi i m/n} (objective.cu smem_fft)
   float* d_beam_x = nullptr;     // [N] beam_coord of each column (attenuation)
   float* d_beam_y = nullptr;     // [M] beam_coord of each row
   float* d_rot_u = nullptr;      // [N] phase_rotate's u of each column (k_cols_fft)

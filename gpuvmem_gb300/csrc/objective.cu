@@ -13,8 +13,12 @@
 //                   sums combined in FP64, weighted residuals stored for
 //                   DChi2.
 //
-// No per-call allocation, no host synchronisation except the single scalar
-// read-back at the end of an evaluation.
+// The FFT passes are radix-8 Stockham passes in shared memory with the
+// butterflies in registers (four passes and barriers for a 2048-point line
+// instead of eleven radix-2 stages).  Images up to 512 x 512 run the three
+// passes and the prior values as one cooperative launch
+// (k_objective_fused).  No per-call allocation, no host synchronisation
+// except the single scalar read-back at the end of an evaluation.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -29,49 +33,115 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__device__ __forceinline__ unsigned bitrev(unsigned x, int bits) {
-  return __brev(x) >> (32 - bits);
+// R-point inverse DFT (exp(+2 pi i r s / R), R = 2^LR <= 8) of v in
+// registers, radix-2 decimation in frequency: the result is in bit-reversed
+// order (X[r] = v[brev(r)]).  The twiddles are 1, i and (+-1 + i)/sqrt(2):
+// multiplications by 1 and i are exact.
+__device__ __forceinline__ float2 rot_turn(float2 d, int s, int m) {
+  // d * e^{2 pi i s / m}, m in {2, 4, 8}, s < m / 2 (compile-time after
+  // unrolling)
+  const float c = 0.70710678118654752440f;
+  if (s == 0) return d;
+  if (m == 4 || s == 2) return make_float2(-d.y, d.x);                 // * i
+  if (s == 1) return make_float2(c * (d.x - d.y), c * (d.x + d.y));    // * (1 + i)/sqrt 2
+  return make_float2(c * (-d.x - d.y), c * (d.x - d.y));               // * (-1 + i)/sqrt 2
 }
 
-// Shared-memory position of element e of a length-2^log2n column: the low
-// 4 bits are XORed with 4 higher bits, so the bit-reversed scatter (lanes
-// 2^(log2n-5) elements apart, all in one bank pair unswizzled) spreads over
-// all 16 eight-byte slots of a 128-byte row, while runs of consecutive
-// elements stay conflict-free.  A bijection on [0, 2^log2n).
-__device__ __forceinline__ int swz(int e, int log2n) {
-  const int sh = log2n >= 8 ? log2n - 4 : 4;
-  return e ^ ((e >> sh) & 15);
-}
-
-// In-place inverse radix-2 DIT FFT of `ncol` independent columns of length
-// n = 2^log2n held in shared memory (element e of column c at
-// buf[c*n + swz(e)]), input in bit-reversed order, output in natural order.
-// tw is the stage-major twiddle table (stage s at offset 2^(s-1) - 1), so
-// the lanes of a warp read consecutive twiddles instead of a power-of-two
-// stride (bank conflicts).
-__device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restrict__ tw) {
-  const int n = 1 << log2n;
-  const int nb = (n >> 1) * ncol;
-  for (int s = 1; s <= log2n; s++) {
-    const int half = 1 << (s - 1);
-    const float2* __restrict__ tws = tw + (half - 1);
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-      const int col = b >> (log2n - 1);
-      const int bb = b & ((n >> 1) - 1);
-      const int grp = bb >> (s - 1);
-      const int pos = bb & (half - 1);
-      const int e0 = (grp << s) + pos;
-      const int a0 = col * n + swz(e0, log2n);
-      const int a1 = col * n + swz(e0 + half, log2n);
-      const float2 w = tws[pos];
-      const float2 t = cmul(w, buf[a1]);
-      const float2 x0 = buf[a0];
-      buf[a0] = make_float2(x0.x + t.x, x0.y + t.y);
-      buf[a1] = make_float2(x0.x - t.x, x0.y - t.y);
+template <int LR>
+__device__ __forceinline__ void dft_inv(float2 (&v)[1 << LR]) {
+  constexpr int R = 1 << LR;
+#pragma unroll
+  for (int half = R / 2; half >= 1; half >>= 1) {
+#pragma unroll
+    for (int g = 0; g < R; g += 2 * half) {
+#pragma unroll
+      for (int s = 0; s < half; s++) {
+        const float2 a = v[g + s], b = v[g + s + half];
+        v[g + s] = make_float2(a.x + b.x, a.y + b.y);
+        v[g + s + half] = rot_turn(make_float2(a.x - b.x, a.y - b.y), s, 2 * half);
+      }
     }
-    __syncthreads();
   }
 }
+
+template <int LR>
+__device__ __forceinline__ constexpr int brev_c(int r) {
+  int o = 0;
+  for (int b = 0; b < LR; b++) o |= ((r >> b) & 1) << (LR - 1 - b);
+  return o;
+}
+
+// One Stockham autosort pass of radix R = 2^LR over `ncol` columns of length
+// n = 2^log2n in shared memory (column c at buf[c * n], natural order).
+// Work item (c, j), j < n / R, reads x[j + r n/R] (r < R), multiplies by the
+// twiddles e^{2 pi i r k / (Ns R)} with k = j mod Ns (table tw[m] =
+// e^{2 pi i m / n}, read through L1), takes the R-point inverse DFT and
+// writes y[(j / Ns) Ns R + k + r Ns] (Govindaraju et al., "High Performance
+// Discrete Fourier Transforms on Graphics Processors", SC 2008).  In place:
+// all items are read before a block barrier and written after it, so each
+// thread holds its items' values in registers: max(VPT, R) of them, VPT the
+// values per thread (ncol * n <= VPT * blockDim.x).
+template <int LR, int VPT>
+__device__ __forceinline__ void stockham_pass(float2* buf, int log2n, int ncol, int lNs,
+                                              const float2* __restrict__ tw) {
+  constexpr int R = 1 << LR;
+  constexpr int kMaxItems = VPT / R > 1 ? VPT / R : 1;
+  const int lq = log2n - LR;  // log2 of the items per column
+  const int items = ncol << lq;
+  float2 v[kMaxItems][R];
+#pragma unroll
+  for (int t = 0; t < kMaxItems; t++) {
+    const int it = threadIdx.x + t * blockDim.x;
+    if (it < items) {
+      const int c = it >> lq, j = it & ((1 << lq) - 1);
+      const float2* x = buf + (c << log2n) + j;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[t][r] = x[r << lq];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < kMaxItems; t++) {
+    const int it = threadIdx.x + t * blockDim.x;
+    if (it < items) {
+      const int c = it >> lq, j = it & ((1 << lq) - 1);
+      const int k = j & ((1 << lNs) - 1);
+      if (lNs > 0) {
+        const int step = k << (log2n - lNs - LR);  // r k n / (Ns R) = r * step
+#pragma unroll
+        for (int r = 1; r < R; r++) v[t][r] = cmul(v[t][r], __ldg(tw + r * step));
+      }
+      dft_inv<LR>(v[t]);
+      float2* y = buf + (c << log2n) + ((j >> lNs) << (lNs + LR)) + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) y[r << lNs] = v[t][brev_c<LR>(r)];
+    }
+  }
+  __syncthreads();
+}
+
+// In-place inverse FFT (cuFFT's CUFFT_INVERSE convention: exp(+i),
+// unnormalised) of `ncol` independent columns of length n = 2^log2n held in
+// shared memory (column c at buf[c * n]), natural order in and out: radix-8
+// Stockham passes, then one of radix 4 or 2.  The caller has synchronised
+// the block after filling buf; needs ncol * n <= VPT * blockDim.x and
+// n <= 2 * blockDim.x * max(1, VPT / 2).
+template <int VPT>
+__device__ void smem_fft(float2* buf, int log2n, int ncol, const float2* __restrict__ tw) {
+  int lNs = 0;
+  while (log2n - lNs >= 3) {
+    stockham_pass<3, VPT>(buf, log2n, ncol, lNs, tw);
+    lNs += 3;
+  }
+  if (log2n - lNs == 2) stockham_pass<2, VPT>(buf, log2n, ncol, lNs, tw);
+  else if (log2n - lNs == 1) stockham_pass<1, VPT>(buf, log2n, ncol, lNs, tw);
+}
+
+// values per thread of the FFT passes: the separate row and column kernels
+// (up to 4096 values over 256 threads) and the fused small-image kernel (up
+// to 512 values over 256 threads)
+constexpr int kVptLarge = 16;
+constexpr int kVptSmall = 2;
 
 // evaluateXt at one pixel (k_eval_xt's arithmetic): xt = pcom + x xicom,
 // plane 0 floored when positivity is on, plane 1 free.
@@ -115,6 +185,7 @@ struct StageParams {
 // Pass 1 for row i of channel c: stage I_nu * A * fg_scale into buf (shared
 // memory, n float2) and FFT the row with the twiddles tw (shared memory);
 // the row goes to grid.  Every thread of the block takes part.
+template <int VPT>
 __device__ __forceinline__ void row_task(const StageParams& sp, const float* __restrict__ chfreq,
                                          float* __restrict__ img, const uint8_t* __restrict__ mask,
                                          const float2* tw, float2* __restrict__ grid, float2* buf,
@@ -156,12 +227,12 @@ __device__ __forceinline__ void row_task(const StageParams& sp, const float* __r
     const float a = attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
     float v = inu * a * sp.fg_scale;
     if (sp.gcf) v *= sp.gcf[q];  // apply_GCF, src/functions.cu:2468
-    buf[swz(bitrev(j, sp.log2n), sp.log2n)] = make_float2(v, 0.0f);
+    buf[j] = make_float2(v, 0.0f);
   }
   __syncthreads();
-  smem_fft(buf, sp.log2n, 1, tw);
+  smem_fft<VPT>(buf, sp.log2n, 1, tw);
   float2* out = grid + (int64_t)c * sp.MN + (int64_t)n * i;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[swz(j, sp.log2n)];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[j];
 }
 
 // Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
@@ -169,11 +240,7 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
                            float* __restrict__ img, const uint8_t* __restrict__ mask,
                            const float2* __restrict__ tw_g, float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
-  const int n = sp.N;
-  float2* buf = sm;
-  float2* tw = sm + n;
-  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
-  row_task(sp, chfreq, img, mask, tw, grid, buf, blockIdx.x, blockIdx.y);
+  row_task<kVptLarge>(sp, chfreq, img, mask, tw_g, grid, sm, blockIdx.x, blockIdx.y);
 }
 
 // Pass 2 for columns j0 .. j0 + cb - 1 of grid G: column FFTs in buf
@@ -181,7 +248,7 @@ __global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
 // 2483-2518) in the reference's float arithmetic.  Load: how the grid is
 // read (plain loads, or L2 loads when the grid was written earlier in the
 // same kernel by other blocks).
-template <bool kL2Loads>
+template <bool kL2Loads, int VPT>
 __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* __restrict__ rot_u,
                                          const float* __restrict__ rot_v, const float2* tw,
                                          float2* __restrict__ G, float2* buf, int j0) {
@@ -189,10 +256,10 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
     const float2* src = G + (int64_t)n * r + j0 + cc;
-    buf[cc * n + swz(bitrev(r, log2n), log2n)] = kL2Loads ? __ldcg(src) : *src;
+    buf[cc * n + r] = kL2Loads ? __ldcg(src) : *src;
   }
   __syncthreads();
-  smem_fft(buf, log2n, cb, tw);
+  smem_fft<VPT>(buf, log2n, cb, tw);
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
     const int r = idx / cb, cc = idx - r * cb;
     const int j = j0 + cc;
@@ -203,7 +270,7 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
     const float phase = -2.0f * (u + v);
     float s, co;
     sincospif(phase, &s, &co);
-    G[(int64_t)n * r + j] = cmul(buf[cc * n + swz(r, log2n)], make_float2(co, s));
+    G[(int64_t)n * r + j] = cmul(buf[cc * n + r], make_float2(co, s));
   }
 }
 
@@ -212,11 +279,7 @@ __global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __
                            const float* __restrict__ rot_v, const float2* __restrict__ tw_g,
                            float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
-  const int n = N;
-  float2* buf = sm;
-  float2* tw = sm + (size_t)cb * n;
-  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = tw_g[k];
-  col_task<false>(N, log2n, cb, rot_u, rot_v, tw, grid + (int64_t)blockIdx.y * MN, buf,
+  col_task<false, kVptLarge>(N, log2n, cb, rot_u, rot_v, tw_g, grid + (int64_t)blockIdx.y * MN, sm,
                   blockIdx.x * cb);
 }
 
@@ -624,7 +687,7 @@ struct FusedArgs {
   const float* chfreq;
   float* img;
   const uint8_t* mask;
-  const float2* tw;
+  const float2* tw;  // FFT twiddles e^{2 pi i m / n}
   const float* rot_u;
   const float* rot_v;
   int C;
@@ -639,20 +702,18 @@ struct FusedArgs {
 };
 
 template <class Img>
-__global__ void __launch_bounds__(256) k_objective_fused(FusedArgs<Img> f) {
+__global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
   extern __shared__ float2 sm[];
   const int n = f.sp.N;
-  float2* buf = sm;              // n * cb values
-  float2* tw = sm + n * f.cb;    // n - 1 twiddles
-  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) tw[k] = f.tw[k];
-  __syncthreads();
+  float2* buf = sm;  // n * cb values
+  const float2* tw = f.tw;
   float2* grid = const_cast<float2*>(f.da.grid);
   // A: rows of every channel, then the prior-value tasks
   const int nrow = n * f.C;
   const int ntask_a = nrow + f.nb_prior * f.ps.n;
   for (int t = blockIdx.x; t < ntask_a; t += gridDim.x) {
     if (t < nrow) {
-      row_task(f.sp, f.chfreq, f.img, f.mask, tw, grid, buf, t % n, t / n);
+      row_task<kVptSmall>(f.sp, f.chfreq, f.img, f.mask, tw, grid, buf, t % n, t / n);
     } else {
       const int u = t - nrow;
       prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
@@ -663,7 +724,7 @@ __global__ void __launch_bounds__(256) k_objective_fused(FusedArgs<Img> f) {
   // B: columns
   const int ncg = n / f.cb;
   for (int t = blockIdx.x; t < ncg * f.C; t += gridDim.x) {
-    col_task<true>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, tw, grid + (int64_t)(t / ncg) * f.sp.MN,
+    col_task<true, kVptSmall>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, tw, grid + (int64_t)(t / ncg) * f.sp.MN,
                    buf, (t % ncg) * f.cb);
     __syncthreads();
   }
@@ -723,14 +784,14 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   const int n = P.N, C = (int)P.chans.size();
   const StageParams sp = stage_params(P, flag_opt, write_clip, xs);
   const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
-  const size_t sm1 = sizeof(float2) * (2 * n - 1);
+  const size_t sm1 = sizeof(float2) * n;
   if (sm1 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_rows_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
   k_rows_fft<<<dim3(n, C), threads, sm1, P.stream>>>(sp, P.d_chfreq, d_img, P.d_mask, P.d_twiddle,
                                                      P.d_grid);
   GV_LAUNCH("k_rows_fft");
   const int cb = cols_per_block(n, C, P.num_sms);
-  const size_t sm2 = sizeof(float2) * ((size_t)cb * n + n - 1);
+  const size_t sm2 = sizeof(float2) * (size_t)cb * n;
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
   k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
@@ -810,7 +871,7 @@ static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store
   f.prior_done = P.d_flags + kFlagPriorDone;
   f.bar = P.d_flags + kFlagBarCount;
   f.err = P.d_flags + kFlagErr;
-  const size_t smem = sizeof(float2) * (size_t)(n - 1 + n * f.cb);
+  const size_t smem = sizeof(float2) * (size_t)(n * f.cb);
   int& blocks = P.fused_blocks[ImgKind<Img>::k];
   if (blocks == 0) {
     // every block must be resident at once: at most the occupancy bound,

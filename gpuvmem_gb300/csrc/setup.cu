@@ -1,8 +1,9 @@
 // Problem set-up: the per-problem constants the reference prepares in
 // MFS::setDevice (src/mfs.cu:530-943), laid out for GB300.
 //
-//  * calculateNoiseAndBeam (src/functions.cu:1655-1814) on the host, FP64
-//    moments and the FP32 Neumaier weight sum as the reference.
+//  * calculateNoiseAndBeam (src/functions.cu:1655-1814) on the GPU: FP64
+//    moments in parallel, and the reference's uncompensated FP32 weight sum
+//    as a sequential chain per channel (bit for bit).
 //  * hermitianSymmetry (src/functions.cu:2256-2273) and the vis_mod cell
 //    choice (src/functions.cu:2557-2609) are evaluated once per visibility
 //    (u,v,w are constant), so weights of visibilities outside the grid are
@@ -23,19 +24,68 @@ namespace gv {
 
 namespace {
 
-// Neumaier sum in float, src/functions.cu:353-367 (returns the plain sum).
-float neumaier_f(const float* d, int64_t n) {
-  if (n <= 0) return 0.0f;
-  float sum = d[0], c = 0.0f;
-  for (int64_t i = 1; i < n; i++) {
-    float t = sum + d[i];
-    if (std::fabs(sum) >= std::fabs(d[i]))
-      c += (sum - t) + d[i];
-    else
-      c += (d[i] - t) + sum;
-    sum = t;
+// calculateNoiseAndBeam (src/functions.cu:1700-1814) on the GPU, in two
+// kernels.
+//
+// k_beam_moments: calc_sBeam's weighted second moments of one channel
+// (:1655-1683), sum_k u^2 w, v^2 w, u v w with u, v in wavelengths of the
+// float wavelength, as FP64 block partials; the last block adds the
+// channel's totals to acc[0..2], so channels are added in order.  (The
+// reference adds under an OpenMP reduction, in no fixed order; FP64 keeps
+// the difference at the level of FP64 rounding.)
+__global__ void __launch_bounds__(256) k_beam_moments(int64_t n, float lam,
+                                                      const double* __restrict__ uvw,
+                                                      const float* __restrict__ w,
+                                                      double* __restrict__ part,
+                                                      uint32_t* __restrict__ done,
+                                                      double* __restrict__ acc) {
+  double suu = 0.0, svv = 0.0, suv = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double u = uvw[3 * k] / lam, v = uvw[3 * k + 1] / lam, wk = w[k];
+    suu += u * u * wk;
+    svv += v * v * wk;
+    suv += u * v * wk;
   }
-  return sum;
+  __shared__ double red[3][8];
+  for (int o = 16; o > 0; o >>= 1) {
+    suu += __shfl_down_sync(0xffffffffu, suu, o);
+    svv += __shfl_down_sync(0xffffffffu, svv, o);
+    suv += __shfl_down_sync(0xffffffffu, suv, o);
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][wid] = suu;
+    red[1][wid] = svv;
+    red[2][wid] = suv;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[threadIdx.x][i];
+    part[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+  }
+  if (last_block_done(done, gridDim.x) && threadIdx.x < 3) {
+    double t = 0.0;
+    for (unsigned b = 0; b < gridDim.x; b++) t += __ldcg(part + (int64_t)threadIdx.x * gridDim.x + b);
+    acc[threadIdx.x] += t;
+  }
+}
+
+// k_weight_chain: reduceCPU (:353-367) of each channel's weights, one
+// thread per channel.  reduceCPU returns its running FP32 sum without the
+// compensation it computes, i.e. the plain sequential FP32 sum; a
+// sequential chain reproduces it bit for bit (a parallel tree would round
+// differently).
+__global__ void k_weight_chain(int C, const int64_t* __restrict__ off,
+                               const float* __restrict__ w, float* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int64_t o = off[c], n = off[c + 1] - off[c];
+  float s = n > 0 ? w[o] : 0.0f;
+#pragma unroll 8
+  for (int64_t k = 1; k < n; k++) s = __fadd_rn(s, w[o + k]);
+  out[c] = s;
 }
 
 __global__ void k_prepare_vis(int64_t n, int64_t off, int chan, float freq,
@@ -312,44 +362,6 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     return GV_ERR_INVALID;
   }
 
-  // ---- calculateNoiseAndBeam on the host ----------------------------------
-  {
-    float sum_w = 0.0f;
-    double s_uu = 0.0, s_vv = 0.0, s_uv = 0.0;
-    for (int c = 0; c < C; c++) {
-      const gv_channel_desc& ch = d.channels[c];
-      if (ch.nvis <= 0) continue;
-      const float lam = wavelength(ch.freq_hz);
-      double luu = 0.0, lvv = 0.0, luv = 0.0;
-      for (int64_t k = 0; k < ch.nvis; k++) {
-        const double u = ch.uvw[3 * k] / lam, v = ch.uvw[3 * k + 1] / lam;
-        const double w = ch.weight[k];
-        luu += u * u * w;
-        lvv += v * v * w;
-        luv += u * v * w;
-      }
-      s_uu += luu;
-      s_vv += lvv;
-      s_uv += luv;
-      sum_w += neumaier_f(ch.weight, ch.nvis);
-    }
-    if (!(sum_w > 0.0f)) {
-      set_error("The sum of the visibility weights cannot be zero");  // functions.cu:1790
-      return GV_ERR_INVALID;
-    }
-    s_uu /= sum_w;
-    s_vv /= sum_w;
-    s_uv /= sum_w;
-    const float variance = 1.0f / sum_w;
-    const double uu_mv = s_uu - s_vv, uu_pv = s_uu + s_vv;
-    const double sq = std::sqrt(uu_mv * uu_mv + 4.0 * s_uv * s_uv);
-    P.bmaj = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv - sq)) / kRpDegD;
-    P.bmin = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv + sq)) / kRpDegD;
-    P.bpa = (-0.5 * std::atan2(2.0 * s_uv, uu_mv)) / kRpDegD;
-    P.sum_weights = sum_w;
-    P.vis_noise = d.vis_noise > 0.0f ? d.vis_noise : 0.5f * sqrtf(variance);
-  }
-
   const int64_t MN = (int64_t)P.M * P.N;
   cudaStream_t st = P.stream;
 
@@ -357,7 +369,11 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
   {
     double* d_uvw = nullptr;
     float2* d_vo_in = nullptr;
-    float* d_w_in = nullptr;
+    float* d_w_in = nullptr;      // [V] weights of all channels, as given
+    double* d_mom = nullptr;      // beam moments: [3] totals, then 3 * nbm partials
+    uint32_t* d_mdone = nullptr;
+    float* d_wsum = nullptr;      // [C] reduceCPU of each channel's weights
+    int64_t* d_off = nullptr;     // [C + 1]
     float4* deg_u = nullptr;
     float2* vo_u = nullptr;
     uint4* ph_u = nullptr;
@@ -371,6 +387,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     for (auto& ch : P.chans) maxc = std::max(maxc, ch.nvis);
     auto cleanup = [&]() {
       cudaFree(d_uvw); cudaFree(d_vo_in); cudaFree(d_w_in); cudaFree(deg_u);
+      cudaFree(d_mom); cudaFree(d_mdone); cudaFree(d_wsum); cudaFree(d_off);
       cudaFree(vo_u); cudaFree(ph_u); cudaFree(wl_u); cudaFree(E_u); cudaFree(keys); cudaFree(keys2);
       cudaFree(idx); cudaFree(tmp);
     };
@@ -384,7 +401,20 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
   } while (0)
     GV_SETUP_CUDA(cudaMalloc(&d_uvw, sizeof(double) * 3 * std::max<int64_t>(maxc, 1)));
     GV_SETUP_CUDA(cudaMalloc(&d_vo_in, sizeof(float2) * std::max<int64_t>(maxc, 1)));
-    GV_SETUP_CUDA(cudaMalloc(&d_w_in, sizeof(float) * std::max<int64_t>(maxc, 1)));
+    GV_SETUP_CUDA(cudaMalloc(&d_w_in, sizeof(float) * V));
+    const int nbm = 4 * P.num_sms;
+    GV_SETUP_CUDA(cudaMalloc(&d_mom, sizeof(double) * (3 + 3 * (size_t)nbm)));
+    GV_SETUP_CUDA(cudaMemsetAsync(d_mom, 0, sizeof(double) * 3, st));
+    GV_SETUP_CUDA(cudaMalloc(&d_mdone, sizeof(uint32_t)));
+    GV_SETUP_CUDA(cudaMemsetAsync(d_mdone, 0, sizeof(uint32_t), st));
+    GV_SETUP_CUDA(cudaMalloc(&d_wsum, sizeof(float) * C));
+    GV_SETUP_CUDA(cudaMalloc(&d_off, sizeof(int64_t) * (C + 1)));
+    {
+      std::vector<int64_t> off(C + 1, 0);
+      for (int c = 0; c < C; c++) off[c + 1] = off[c] + P.chans[c].nvis;
+      GV_SETUP_CUDA(cudaMemcpy(d_off, off.data(), sizeof(int64_t) * (C + 1),
+                               cudaMemcpyHostToDevice));
+    }
     GV_SETUP_CUDA(cudaMalloc(&deg_u, sizeof(float4) * V));
     GV_SETUP_CUDA(cudaMalloc(&vo_u, sizeof(float2) * V));
     GV_SETUP_CUDA(cudaMalloc(&ph_u, sizeof(uint4) * V));
@@ -401,13 +431,49 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
                                     cudaMemcpyHostToDevice, st));
       GV_SETUP_CUDA(cudaMemcpyAsync(d_vo_in, ch.vo, sizeof(float2) * ch.nvis,
                                     cudaMemcpyHostToDevice, st));
-      GV_SETUP_CUDA(cudaMemcpyAsync(d_w_in, ch.weight, sizeof(float) * ch.nvis,
+      float* w_c = d_w_in + P.chans[c].off;
+      GV_SETUP_CUDA(cudaMemcpyAsync(w_c, ch.weight, sizeof(float) * ch.nvis,
                                     cudaMemcpyHostToDevice, st));
       const int bs = 256;
+      // calc_sBeam of this channel (the uvw buffer is reused per channel)
+      const unsigned mb = (unsigned)std::min<int64_t>((ch.nvis + bs - 1) / bs, nbm);
+      k_beam_moments<<<mb, bs, 0, st>>>(ch.nvis, wavelength(ch.freq_hz), d_uvw, w_c, d_mom + 3,
+                                        d_mdone, d_mom);
+      GV_SETUP_CUDA(cudaGetLastError());
       k_prepare_vis<<<(unsigned)((ch.nvis + bs - 1) / bs), bs, 0, st>>>(
-          ch.nvis, P.chans[c].off, c, ch.freq_hz, d_uvw, d_vo_in, d_w_in, P.deltau,
+          ch.nvis, P.chans[c].off, c, ch.freq_hz, d_uvw, d_vo_in, w_c, P.deltau,
           P.deltav, P.N, P.dx_rad, P.dy_rad, deg_u, vo_u, ph_u, wl_u, E_u, keys, idx);
       GV_SETUP_CUDA(cudaGetLastError());
+    }
+    // calculateNoiseAndBeam's weight sum: reduceCPU per channel, added over
+    // the channels in FP32 in order (src/functions.cu:1731-1733)
+    k_weight_chain<<<(C + 31) / 32, 32, 0, st>>>(C, d_off, d_w_in, d_wsum);
+    GV_SETUP_CUDA(cudaGetLastError());
+    {
+      std::vector<float> wsum(C);
+      double mom[3];
+      GV_SETUP_CUDA(cudaMemcpyAsync(wsum.data(), d_wsum, sizeof(float) * C,
+                                    cudaMemcpyDeviceToHost, st));
+      GV_SETUP_CUDA(cudaMemcpyAsync(mom, d_mom, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+      GV_SETUP_CUDA(cudaStreamSynchronize(st));
+      float sum_w = 0.0f;
+      for (int c = 0; c < C; c++)
+        if (P.chans[c].nvis > 0) sum_w += wsum[c];
+      if (!(sum_w > 0.0f)) {
+        cleanup();
+        set_error("The sum of the visibility weights cannot be zero");  // functions.cu:1790
+        return GV_ERR_INVALID;
+      }
+      // calc_beamSize (:1685-1698) and the noise (:1796-1811)
+      const double s_uu = mom[0] / sum_w, s_vv = mom[1] / sum_w, s_uv = mom[2] / sum_w;
+      const float variance = 1.0f / sum_w;
+      const double uu_mv = s_uu - s_vv, uu_pv = s_uu + s_vv;
+      const double sq = std::sqrt(uu_mv * uu_mv + 4.0 * s_uv * s_uv);
+      P.bmaj = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv - sq)) / kRpDegD;
+      P.bmin = (1.0 / std::sqrt(2.0) / kPiD / std::sqrt(uu_pv + sq)) / kRpDegD;
+      P.bpa = (-0.5 * std::atan2(2.0 * s_uv, uu_mv)) / kRpDegD;
+      P.sum_weights = sum_w;
+      P.vis_noise = d.vis_noise > 0.0f ? d.vis_noise : 0.5f * sqrtf(variance);
     }
     GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, idx,
                                                   P.d_perm, (int64_t)V, 0, 64, st));
@@ -505,18 +571,14 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
 
   // ---- FFT twiddles, grids, reduction scratch -----------------------------
   {
-    // stage-major: stage s (half = 2^(s-1)) holds e^{+2 pi i pos (n >> s) / n}
-    // for pos < half at offset half - 1, so a stage reads consecutive entries
-    std::vector<float2> tw(n - 1);
-    for (int half = 1; half < n; half <<= 1) {
-      const int tstride = n / (2 * half);
-      for (int pos = 0; pos < half; pos++) {
-        const double a = 2.0 * kPiD * (pos * tstride) / n;
-        tw[half - 1 + pos] = make_float2((float)std::cos(a), (float)std::sin(a));
-      }
+    // e^{+2 pi i m / n}, m < n (the FFT passes' twiddles, FP64 rounded once)
+    std::vector<float2> tw(n);
+    for (int m = 0; m < n; m++) {
+      const double a = 2.0 * kPiD * m / n;
+      tw[m] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
-    GV_CUDA(cudaMalloc(&P.d_twiddle, sizeof(float2) * (n - 1)));
-    GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * (n - 1),
+    GV_CUDA(cudaMalloc(&P.d_twiddle, sizeof(float2) * n));
+    GV_CUDA(cudaMemcpyAsync(P.d_twiddle, tw.data(), sizeof(float2) * n,
                             cudaMemcpyHostToDevice, st));
   }
   {

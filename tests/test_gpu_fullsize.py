@@ -346,3 +346,20 @@ def test_mfs1024_planes_sampled(mfs1024, flag):
           f"{e_c:.2e}; gradient plane {plane} {e_g:.2e} of max at {pix.size} pixels")
     assert e_c <= CHI2_RTOL
     assert e_g <= GRAD_TOL
+
+
+# ---- calculateNoiseAndBeam on the GPU ---------------------------------------
+
+@pytest.mark.parametrize("which", ["plain256", "plain2048"])
+def test_noise_and_beam_on_gpu(which, request):
+    """calculateNoiseAndBeam (src/functions.cu:1700-1814): the FP32 weight
+    sum (the reference's uncompensated sequential sum) bit for bit, the beam
+    moments and the visibility noise against the oracle."""
+    data, orc, prob = request.getfixturevalue(which)
+    inf = prob.info
+    assert np.float32(inf.sum_weights).tobytes() == np.float32(orc.sum_weights).tobytes(), \
+        (inf.sum_weights, orc.sum_weights)
+    for a, b in ((inf.beam_bmaj_deg, orc.bmaj), (inf.beam_bmin_deg, orc.bmin),
+                 (inf.beam_bpa_deg, orc.bpa)):
+        assert abs(a - b) <= 1e-9 * max(abs(b), 1e-30), (a, b)
+    assert np.float32(inf.vis_noise).tobytes() == np.float32(orc.vis_noise).tobytes()
