@@ -238,6 +238,24 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def cufft_inverse_2d(C, n, stream, reps=5):
+    """Device time of cuFFT's unnormalised inverse 2-D C2C transform of C
+    grids of n x n complex64 (the comparison the FFT passes stand against)."""
+    import torch
+    x = torch.randn(C, n, n, dtype=torch.complex64, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            torch.fft.ifft2(x, norm="forward")
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(reps)]
+        for a, b in ev:
+            a.record(stream)
+            torch.fft.ifft2(x, norm="forward")
+            b.record(stream)
+    torch.cuda.synchronize()
+    return statistics.median(a.elapsed_time(b) for a, b in ev) / 1e3
+
+
 def reference_cuda(data, img, band_rows):
     """The reference's own kernels on this GPU (oracle/ref_harness): device
     time of chi2() (src/functions.cu:4323-4454) and of dchi2()
@@ -405,6 +423,7 @@ def run_ours(args):
         b.record(stream)
     torch.cuda.synchronize()
     t_obj = statistics.median(a.elapsed_time(b) for a, b in evo) / 1e3
+    t_cufft = cufft_inverse_2d(len(data.freqs), cfg.n, stream)
 
     # end to end through the public API with host buffers
     h_img = torch.empty(img.shape, dtype=torch.float32).pin_memory()
@@ -444,7 +463,12 @@ def run_ours(args):
     obj = {"ms": 1e3 * t_obj, "degridded_vis_per_s": data.nvis / t_obj,
            "algorithmic_bytes": obj_bytes, "achieved_gbs": obj_bytes / t_obj / 1e9,
            "hbm_peak_gbs": peaks["hbm_gbs"], "frac": obj_bytes / t_obj / 1e9 / peaks["hbm_gbs"],
-           "note": "8 MN + 16 MN per channel + 28 B per visibility"}
+           "note": "8 MN + 16 MN per channel + 28 B per visibility",
+           "cufft_inverse_2d_ms": 1e3 * t_cufft,
+           "cufft_note": "cuFFT (torch.fft.ifft2, unnormalised) of the same C x N x N complex64 "
+                         "grids, for comparison with the two FFT passes of the objective (which "
+                         "also stage the image and apply the phase rotation); not on the "
+                         "product path"}
     cpu = cpu_baseline(data, terms, args.cpu_sample_s)
     refc = None
     if not args.no_reference_cuda:

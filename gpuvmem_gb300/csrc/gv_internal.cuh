@@ -149,8 +149,8 @@ struct Problem {
   size_t epi_bytes = 0;
   int degrid_threads = 256;      // k_degrid block size
   int degrid_blocks = 0;         // k_degrid blocks per channel cap (0: part_stride)
-  int fused = 1;                 // small images: the objective as one cooperative launch
-                                 // (GV_FUSED=0 at creation turns it off)
+  int fused = 0;                 // small images: the objective as one cooperative launch
+                                 // (GV_FUSED=1 at creation turns it on)
   int fused_off = 0;             // > 0 while callers that run problems concurrently launch
   int fused_blocks[3] = {0, 0, 0};  // cooperative blocks of k_objective_fused (per image kind)
   void* graphs = nullptr;        // graph cache (graph.cu)
@@ -321,6 +321,17 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
 gv_status prior_value_launch(Problem& P, int t, const float* d_img, int slot);
 gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi);
 gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_res);
+// Batches: the objectives of several problems (store_res on) in one
+// cooperative launch.  batch_objective_args writes a problem's arguments
+// (batch_arg_bytes() bytes, host) and its task counts per phase, or returns
+// GV_ERR_UNSUPPORTED when the problem cannot run there (image above 512,
+// priors before Chi2); batch_objective_launch runs np problems whose
+// arguments and [3][np + 1] task offsets are in device memory.
+size_t batch_arg_bytes();
+gv_status batch_objective_args(Problem& P, float* d_img, int flag_opt, void* out, int tasks[3]);
+gv_status batch_objective_launch(int np, const void* d_args, const int* d_off, int max_n,
+                                 int max_tasks, uint32_t* d_bar, uint32_t* d_err, int num_sms,
+                                 cudaStream_t st);
 gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
                               cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 gv_status fetch_scalars(Problem& P, int n);

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 
 #include "gv_internal.cuh"
 
@@ -734,6 +735,80 @@ __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
     degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C);
 }
 
+// ---- batches: the objectives of several problems in one cooperative launch
+//
+// k_objective_fused_batch runs k_objective_fused's three phases over the
+// tasks of every problem of a batch: off[] holds, per phase, the prefix sums
+// of the problems' task counts (an offset table), and a block finds the
+// problem of its task by binary search.  Each task is the same block
+// computation with the same partial slots as in the single-problem launch,
+// so every problem's values are bit-identical to its own launch.
+
+template <class Img>
+struct FusedBatch {
+  const FusedArgs<Img>* args;  // [np] per-problem arguments (device memory)
+  const int* off;              // [3][np + 1] task offsets of phases A, B, C
+  int np;
+  int clear_cmax;              // zero every problem's max |w Vr| word first
+  uint32_t* bar;               // [2] grid barrier
+  uint32_t* err;
+};
+
+__device__ __forceinline__ int task_problem(const int* off, int np, int t) {
+  int lo = 0, hi = np;  // off[lo] <= t < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <class Img>
+__global__ void __launch_bounds__(256, 2) k_objective_fused_batch(FusedBatch<Img> fb) {
+  extern __shared__ float2 sm[];
+  const int* offA = fb.off;
+  const int* offB = fb.off + fb.np + 1;
+  const int* offC = fb.off + 2 * (fb.np + 1);
+  if (fb.clear_cmax && blockIdx.x == 0)
+    for (int p = threadIdx.x; p < fb.np; p += blockDim.x) *fb.args[p].da.cmax = 0u;
+  // A: rows of every channel of every problem, then its prior-value tasks
+  for (int t = blockIdx.x; t < __ldg(offA + fb.np); t += gridDim.x) {
+    const int p = task_problem(offA, fb.np, t);
+    const FusedArgs<Img>& f = fb.args[p];
+    const int u = t - __ldg(offA + p);
+    const int n = f.sp.N, nrow = n * f.C;
+    if (u < nrow) {
+      row_task<kVptSmall>(f.sp, f.chfreq, f.img, f.mask, f.tw, const_cast<float2*>(f.da.grid),
+                          sm, u % n, u / n);
+    } else {
+      const int v = u - nrow;
+      prior_task(f.ps, f.mask, f.prior_done, v % f.nb_prior, f.nb_prior, v / f.nb_prior);
+    }
+    __syncthreads();
+  }
+  if (!grid_barrier(fb.bar, fb.err)) return;
+  // B: columns
+  for (int t = blockIdx.x; t < __ldg(offB + fb.np); t += gridDim.x) {
+    const int p = task_problem(offB, fb.np, t);
+    const FusedArgs<Img>& f = fb.args[p];
+    const int u = t - __ldg(offB + p);
+    const int n = f.sp.N, ncg = n / f.cb;
+    col_task<true, kVptSmall>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, f.tw,
+                              const_cast<float2*>(f.da.grid) + (int64_t)(u / ncg) * f.sp.MN, sm,
+                              (u % ncg) * f.cb);
+    __syncthreads();
+  }
+  if (!grid_barrier(fb.bar, fb.err)) return;
+  // C: degridding and chi2
+  for (int t = blockIdx.x; t < __ldg(offC + fb.np); t += gridDim.x) {
+    const int p = task_problem(offC, fb.np, t);
+    const FusedArgs<Img>& f = fb.args[p];
+    const int u = t - __ldg(offC + p);
+    degrid_task<true>(f.da, u % f.nb_deg, f.nb_deg, u / f.nb_deg, f.C);
+  }
+}
+
 }  // namespace
 
 // Columns per block of the column pass: 4096 / n (4K complex values of
@@ -850,10 +925,10 @@ struct ImgKind<XtImage> {
 // The objective's passes (and the prior values of ps) in one cooperative
 // launch; same outputs as model_grids_launch + k_degrid (+ k_prior_values).
 template <class Img>
-static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
-                              const XtSource* xs, double* term_out, uint32_t zero_terms,
-                              const PriorSet<Img>& ps) {
-  const int n = P.N, C = (int)P.chans.size();
+static FusedArgs<Img> fused_args(Problem& P, float* d_img, int flag_opt, bool store_res,
+                                 const XtSource* xs, double* term_out, uint32_t zero_terms,
+                                 const PriorSet<Img>& ps) {
+  const int C = (int)P.chans.size();
   FusedArgs<Img> f{};
   f.sp = stage_params(P, flag_opt, 1, xs);
   f.chfreq = P.d_chfreq;
@@ -871,6 +946,15 @@ static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store
   f.prior_done = P.d_flags + kFlagPriorDone;
   f.bar = P.d_flags + kFlagBarCount;
   f.err = P.d_flags + kFlagErr;
+  return f;
+}
+
+template <class Img>
+static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
+                              const XtSource* xs, double* term_out, uint32_t zero_terms,
+                              const PriorSet<Img>& ps) {
+  const int n = P.N, C = (int)P.chans.size();
+  const FusedArgs<Img> f = fused_args(P, d_img, flag_opt, store_res, xs, term_out, zero_terms, ps);
   const size_t smem = sizeof(float2) * (size_t)(n * f.cb);
   int& blocks = P.fused_blocks[ImgKind<Img>::k];
   if (blocks == 0) {
@@ -979,6 +1063,85 @@ gv_status prior_grad_launch(Problem& P, int t, const float* d_img, float* d_dphi
   return GV_OK;
 }
 
+// The active priors of an objective whose first term is Chi2 (so they see
+// the clipped image) as one prior set over the clipped image d_img; false
+// when the terms do not have that form.
+static bool clip_prior_set(Problem& P, float* d_img, int flag_opt, uint32_t zero,
+                           PriorSet<ClipImage>* ps) {
+  if (P.terms.empty() || P.terms[0].kind != GV_FI_CHI2) return false;
+  const int64_t MN = (int64_t)P.M * P.N;
+  const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
+                    flag_opt};
+  *ps = PriorSet<ClipImage>{};
+  for (size_t t = 1; t < P.terms.size(); t++) {
+    const Term& tm = P.terms[t];
+    if (tm.kind == GV_FI_CHI2) return false;
+    if (zero & (1u << t)) continue;
+    const int k = ps->n++;
+    ps->pp[k] = prior_params(P, tm);
+    ps->img[k] = ClipImage{d_img, P.d_mask, MN, cr, tm.image_index};
+    ps->part[k] = prior_part(P, (int)t);
+    ps->out[k] = P.d_scal + kSlotTerm0 + t;
+  }
+  return true;
+}
+
+// Iteration gating of the objective: the priors Chi2's kernel zeroes.
+static uint32_t gated_terms(const Problem& P) {
+  uint32_t zero = 0u;
+  for (size_t t = 0; t < P.terms.size(); t++)
+    if (P.terms[t].kind != GV_FI_CHI2 && !(P.iteration > 0 && P.terms[t].lambda != 0.0f))
+      zero |= 1u << t;
+  return zero;
+}
+
+size_t batch_arg_bytes() { return sizeof(FusedArgs<ClipImage>); }
+
+gv_status batch_objective_args(Problem& P, float* d_img, int flag_opt, void* out,
+                               int tasks[3]) {
+  if (!(P.N <= 512 && P.degrid_threads == 256)) return GV_ERR_UNSUPPORTED;
+  const uint32_t zero = gated_terms(P);
+  PriorSet<ClipImage> ps{};
+  if (!clip_prior_set(P, d_img, flag_opt, zero, &ps)) return GV_ERR_UNSUPPORTED;
+  const FusedArgs<ClipImage> f =
+      fused_args(P, d_img, flag_opt, true, nullptr, P.d_scal + kSlotTerm0, zero, ps);
+  const int C = (int)P.chans.size();
+  tasks[0] = P.N * C + f.nb_prior * ps.n;
+  tasks[1] = (P.N / f.cb) * C;
+  tasks[2] = f.nb_deg * C;
+  std::memcpy(out, &f, sizeof(f));
+  return GV_OK;
+}
+
+gv_status batch_objective_launch(int np, const void* d_args, const int* d_off, int max_n,
+                                 int max_tasks, uint32_t* d_bar, uint32_t* d_err, int num_sms,
+                                 cudaStream_t st) {
+  FusedBatch<ClipImage> fb{static_cast<const FusedArgs<ClipImage>*>(d_args), d_off, np, 1, d_bar,
+                           d_err};
+  const size_t smem = sizeof(float2) * (size_t)max_n;
+  int occ = 0;
+  GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_objective_fused_batch<ClipImage>,
+                                                        256, smem));
+  if (occ < 1) {
+    set_error("k_objective_fused_batch does not fit on an SM");
+    return GV_ERR_UNSUPPORTED;
+  }
+  const int blocks = std::max(1, std::min(num_sms * std::min(occ, 2), max_tasks));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GV_CUDA(cudaLaunchKernelEx(&cfg, k_objective_fused_batch<ClipImage>, fb));
+  GV_LAUNCH("k_objective_fused_batch");
+  return GV_OK;
+}
+
 // ObjectiveFunction::calcFunction; values land in d_scal[kSlotTerm0 + t].
 // Terms are evaluated in list order; consecutive active priors share one
 // launch.
@@ -991,28 +1154,9 @@ gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_re
     if (P.terms[t].kind == GV_FI_CHI2) has_chi2 = true;
     else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) zero |= 1u << t;
   }
-  if (fused_ok(P) && !P.terms.empty() && P.terms[0].kind == GV_FI_CHI2) {
-    // Chi2 first, so the priors see the clipped image: every active prior
-    // rides in the same cooperative launch
-    PriorSet<ClipImage> ps{};
-    const int64_t MN = (int64_t)P.M * P.N;
-    const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
-                      flag_opt};
-    bool fits = true;
-    for (size_t t = 1; t < P.terms.size(); t++) {
-      const Term& tm = P.terms[t];
-      if (tm.kind == GV_FI_CHI2) fits = false;
-      if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
-      const int k = ps.n++;
-      ps.pp[k] = prior_params(P, tm);
-      ps.img[k] = ClipImage{d_img, P.d_mask, MN, cr, tm.image_index};
-      ps.part[k] = prior_part(P, (int)t);
-      ps.out[k] = P.d_scal + kSlotTerm0 + t;
-    }
-    if (fits)
-      return fused_launch(P, d_img, flag_opt, store_res, nullptr, P.d_scal + kSlotTerm0, zero,
-                          ps);
-  }
+  PriorSet<ClipImage> ps{};
+  if (fused_ok(P) && clip_prior_set(P, d_img, flag_opt, zero, &ps))
+    return fused_launch(P, d_img, flag_opt, store_res, nullptr, P.d_scal + kSlotTerm0, zero, ps);
   int run[kMaxTerms], slots[kMaxTerms], nrun = 0;
   auto flush = [&]() -> gv_status {
     const int n = nrun;
