@@ -761,7 +761,7 @@ class Solver {
     for (int it = 1; it <= o_.total_iterations; it++) {
       rep->iterations = it;
       GV_TRY(linmin(img, w_.xi, &fret));
-      if (it >= 2 && (double)fret <= f_target_) {
+      if ((it >= 2 || first_iter_ > 0) && (double)fret <= f_target_) {
         rep->exit_reason = 4;
         break;
       }
@@ -813,7 +813,7 @@ class Solver {
       GV_CUDA(cudaMemcpyAsync(w_.p_old, img, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
       GV_CUDA(cudaMemcpyAsync(w_.xi_old, w_.xi, sizeof(float) * PMN, cudaMemcpyDeviceToDevice, P_.stream));
       GV_TRY(linmin(img, w_.xi, &fret));
-      if (it >= 2 && (double)fret <= f_target_) {
+      if ((it >= 2 || first_iter_ > 0) && (double)fret <= f_target_) {
         rep->exit_reason = 4;
         break;
       }

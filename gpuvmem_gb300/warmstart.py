@@ -71,10 +71,38 @@ def load_sky(seed: int, base: synth.SynthConfig = CONFIG4, device="cuda") -> Sky
     return Sky(seed, prob, x, d, float(info.fg_scale), float(info.minpix))
 
 
+# restarts of frprmn after a stall (see solve)
+RESTARTS = 3
+
+
+def solve(sky: Sky, img, iterations: int, ftol=1e-12, f_target=-np.inf,
+          priors_from_start=False, restarts=RESTARTS):
+    """frprmn from img (in place) to convergence, as the solver of both the
+    plain and the warm runs.  frprmn ends on ftol when a line search finds
+    no decrease at all; with an inexact float line search and the
+    positivity floor a conjugate direction can lose descent that way well
+    above the optimum.  After such a stop the solver is restarted from where
+    it stopped (steepest descent, the priors active), at most `restarts`
+    times; a restart that cannot move ends it.  Stops early once
+    f <= f_target.  Returns (report of the last leg, iterations in all,
+    restarts used)."""
+    total, k, rep = 0, 0, None
+    while True:
+        sky.prob.set_iteration(1 if (priors_from_start or k > 0) else 0)
+        rep = sky.prob.optimize_until(img, f_target, "CG-FRPRMN", iterations=iterations - total,
+                                      ftol=ftol, priors_from_start=priors_from_start or k > 0)
+        total += rep.iterations
+        if rep.exit_reason != 1 or total >= iterations or k >= restarts:
+            break
+        if k > 0 and rep.iterations <= 1:
+            break
+        k += 1
+    return rep, total, k
+
+
 def plain_solve(sky: Sky, iterations: int, ftol: float):
     img = sky.prob.initial_image()
-    sky.prob.set_iteration(0)
-    rep = sky.prob.optimize(img, "CG-FRPRMN", iterations=iterations, ftol=ftol)
+    rep, _, _ = solve(sky, img, iterations, ftol=ftol)
     return img, rep
 
 
@@ -236,15 +264,17 @@ def choose_start(sky: Sky, net: UNet, scales=SCALES, cuts=CUTS):
 
 
 def time_to_target(sky: Sky, start, f_target: float, max_iter: int, priors_from_start=False):
+    """Wall time of solve() from `start` until f <= f_target; returns (time,
+    report with .iterations the total over restarts, reached, restarts)."""
     import torch
-    sky.prob.set_iteration(0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    rep = sky.prob.optimize_until(start, f_target, "CG-FRPRMN", iterations=max_iter,
-                                  priors_from_start=priors_from_start)
+    rep, total, k = solve(sky, start, max_iter, f_target=f_target,
+                          priors_from_start=priors_from_start)
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
-    return t, rep, bool(rep.exit_reason == 4 or rep.f_final <= f_target)
+    rep.iterations = total
+    return t, rep, bool(rep.exit_reason == 4 or rep.f_final <= f_target), k
 
 
 def evaluate(net: UNet, seeds: Sequence[int], iterations=300, ftol=1e-9, rel=1e-4,
@@ -262,7 +292,7 @@ def evaluate(net: UNet, seeds: Sequence[int], iterations=300, ftol=1e-9, rel=1e-
         _, rep = plain_solve(sky, iterations, ftol)
         f_star = float(rep.f_final)
         target = f_star + rel * abs(f_star)
-        tp, rp, okp = time_to_target(sky, sky.prob.initial_image(), target, iterations)
+        tp, rp, okp, kp = time_to_target(sky, sky.prob.initial_image(), target, iterations)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         start, which, fw, fpl = choose_start(sky, net)
@@ -270,17 +300,18 @@ def evaluate(net: UNet, seeds: Sequence[int], iterations=300, ftol=1e-9, rel=1e-
         t_policy = time.perf_counter() - t0
         # the plain solver from the chosen start, in the reference's order
         # (priors off during the first line search) ...
-        tw, rw, okw = time_to_target(sky, start.clone(), target, iterations)
+        tw, rw, okw, kw = time_to_target(sky, start.clone(), target, iterations)
         # ... and, for comparison, with the priors counting from the start
-        tw1, rw1, okw1 = time_to_target(sky, start.clone(), target, iterations,
-                                        priors_from_start=True)
+        tw1, rw1, okw1, _ = time_to_target(sky, start.clone(), target, iterations,
+                                           priors_from_start=True)
         row = dict(seed=int(s), f_plain_converged=f_star, plain_iterations=int(rep.iterations),
                    t_plain=tp, it_plain=int(rp.iterations), reached_plain=okp,
                    t_warm=t_policy + tw, t_policy=t_policy, it_warm=int(rw.iterations),
                    reached_warm=okw, start=which, f_start_warm=float(fw),
                    f_start_plain=float(fpl), f_warm_final=float(rw.f_final),
                    t_warm_priors_first=t_policy + tw1, it_warm_priors_first=int(rw1.iterations),
-                   reached_warm_priors_first=okw1)
+                   reached_warm_priors_first=okw1, restarts_plain=kp, restarts_warm=kw,
+                   exit_plain=int(rp.exit_reason), exit_warm=int(rw.exit_reason))
         rows.append(row)
         if log:
             log(json.dumps(row))

@@ -238,8 +238,9 @@ gv_status gv_evaluate(gv_problem* p, float* d_img, float* d_xi, int32_t iter,
  * being captured. */
 gv_status gv_problem_set_graphs(gv_problem* p, int32_t enable);
 
-/* gv_optimize that also stops (exit_reason 4) once a line search from the
- * second iteration on reaches f <= f_target (no counterpart in the
+/* gv_optimize that also stops (exit_reason 4) once a line search with the
+ * priors active (from the second iteration on, or from the first with
+ * priors_from_start) reaches f <= f_target (no counterpart in the
  * reference: used to time convergence to a given objective).  With
  * priors_from_start = 0 the priors are off during the first line search, as
  * in the reference (Fi::iteration is 0 until the first calcGradient);
