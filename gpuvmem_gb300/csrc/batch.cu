@@ -1,14 +1,16 @@
 // Batches of independent problems (different sizes and visibility counts)
 // evaluated together.  One objective + gradient evaluation of every problem
-// is captured into a single CUDA graph: the objectives of all problems run as
-// one cooperative launch over an offset table of their tasks
+// is captured into a single CUDA graph: each problem's kernel sequence is a
+// branch forked from one capture stream, together with the copies of its
+// scalars and error word to pinned host memory, so the whole batch runs as
+// one graph launch with the problems' kernels overlapping on the GPU, and one
+// synchronisation.  With GV_BATCH_FUSED=1 the objectives of all problems run
+// instead as one cooperative launch over an offset table of their tasks
 // (k_objective_fused_batch, when every problem is up to 512 x 512 with Chi2
-// as its first term), then each problem's gradient is a branch forked from
-// the capture stream, together with the copies of its scalars and error word
-// to pinned host memory, so the whole batch runs as one graph launch with the
-// problems' kernels overlapping on the GPU, and one synchronisation.  The
-// reference runs problems one after another, each with several host
-// synchronisations per evaluation.
+// as its first term) before the gradient branches; on 64 problems of sides
+// 128-512 the branches are faster (10.3 against 11.1 ms a batch), so they are
+// the default.  The reference runs problems one after another, each with
+// several host synchronisations per evaluation.
 #include <algorithm>
 #include <cstdlib>
 #include <vector>
@@ -43,7 +45,7 @@ struct gv_batch {
   std::vector<BatchGraph> graphs;
   uint64_t clock = 0;
   int use_graph = 1;
-  int fused_objective = 1;  // objectives as one cooperative launch (GV_BATCH_FUSED=0: off)
+  int fused_objective = 0;  // objectives as one cooperative launch (GV_BATCH_FUSED=1: on)
 };
 
 namespace {

@@ -83,8 +83,17 @@ __global__ void k_weight_chain(int C, const int64_t* __restrict__ off,
   if (c >= C) return;
   const int64_t o = off[c], n = off[c + 1] - off[c];
   float s = n > 0 ? w[o] : 0.0f;
-#pragma unroll 8
-  for (int64_t k = 1; k < n; k++) s = __fadd_rn(s, w[o + k]);
+  // the additions stay in order; the loads run 32 ahead so their latency
+  // overlaps (one dependent add per value is then the critical path)
+  int64_t k = 1;
+  for (; k + 32 <= n; k += 32) {
+    float v[32];
+#pragma unroll
+    for (int t = 0; t < 32; t++) v[t] = __ldg(w + o + k + t);
+#pragma unroll
+    for (int t = 0; t < 32; t++) s = __fadd_rn(s, v[t]);
+  }
+  for (; k < n; k++) s = __fadd_rn(s, w[o + k]);
   out[c] = s;
 }
 

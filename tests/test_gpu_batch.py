@@ -29,14 +29,18 @@ def _image(prob, seed):
     return torch.from_numpy(img).cuda()
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_batch_matches_single_problems(graphs):
+@pytest.mark.parametrize("graphs,fused", [(True, False), (True, True), (False, False)])
+def test_batch_matches_single_problems(graphs, fused, monkeypatch):
+    """fused: the objectives of all problems as one cooperative launch over
+    an offset table of their tasks (GV_BATCH_FUSED=1)."""
     import torch
     import gpuvmem_gb300 as gv
-    datas, terms = _setup([64, 128, 128, 256, 64])
+    datas, terms = _setup([64, 128, 128, 256, 64, 512])
     pa = [gv.Problem(d, t) for d, t in zip(datas, terms)]
     pb = [gv.Problem(d, t) for d, t in zip(datas, terms)]
+    monkeypatch.setenv("GV_BATCH_FUSED", "1" if fused else "0")
     batch = gv.Batch(pa)
+    monkeypatch.undo()
     batch.set_graphs(graphs)
     imgs0 = [_image(p, 7 + i) for i, p in enumerate(pa)]
     for it in (0, 1, 2, 2):
