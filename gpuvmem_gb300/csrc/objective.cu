@@ -236,12 +236,95 @@ __device__ __forceinline__ void row_task(const StageParams& sp, const float* __r
   for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[j];
 }
 
-// Pass 1: stage I_nu * A * fg_scale for row i of channel c and FFT the row.
-__global__ void k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
-                           float* __restrict__ img, const uint8_t* __restrict__ mask,
-                           const float2* __restrict__ tw_g, float2* __restrict__ grid) {
-  extern __shared__ float2 sm[];
-  row_task<kVptLarge>(sp, chfreq, img, mask, tw_g, grid, sm, blockIdx.x, blockIdx.y);
+// Pass 1 for row i = blockIdx.x and every channel: the row's pixels (or the
+// line search's xt) are read once -- each thread loads all of its pixels
+// before it stores anything, so the loads are in flight together -- clipped
+// (the clip written back once), then per channel staged as
+// I_nu * A * fg_scale (* GCF) in shared memory and FFT'd into the channel's
+// grid.  The same arithmetic per pixel and channel as row_task.  VPT: the
+// row's values per thread (n / blockDim.x, at least 2).
+template <int VPT>
+__global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
+                                                  int C, float* __restrict__ img,
+                                                  const uint8_t* __restrict__ mask,
+                                                  const float2* __restrict__ tw,
+                                                  float2* __restrict__ grid) {
+  extern __shared__ float2 buf[];  // n values, then the row's clipped I_nu0 and alpha
+  const int n = sp.N, i = blockIdx.x;
+  float* s_i0 = reinterpret_cast<float*>(buf + n);
+  float* s_al = s_i0 + n;
+  const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
+                    sp.flag_opt};
+  const bool from_xt = sp.xs.pcom != nullptr;
+  const float x = from_xt ? *sp.xs.x_dev : 0.0f;
+  {
+    float i0[VPT], al[VPT];
+#pragma unroll
+    for (int k = 0; k < VPT; k++) {
+      const int j = threadIdx.x + k * blockDim.x;
+      if (j < n) {
+        const int64_t q = (int64_t)n * i + j;
+        if (from_xt) {
+          xt_pixel(sp.xs, x, sp.MN, q, i0[k], al[k]);
+        } else {
+          i0[k] = img[q];
+          al[k] = img[sp.MN + q];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < VPT; k++) {
+      const int j = threadIdx.x + k * blockDim.x;
+      if (j < n) {
+        // clip2IWNoise, src/functions.cu:2694-2719 (mutates the image: only
+        // the pixels it changes are written back)
+        const int64_t q = (int64_t)n * i + j;
+        const float i0_in = i0[k], al_in = al[k];
+        clip_pixel(mask[q], cr, i0[k], al[k]);
+        if (sp.write_clip && from_xt) {
+          img[q] = i0[k];
+          img[sp.MN + q] = al[k];
+        } else if (sp.write_clip) {
+          if (i0[k] != i0_in) img[q] = i0[k];
+          if (al[k] != al_in) img[sp.MN + q] = al[k];
+        }
+        s_i0[j] = i0[k];  // read back by this thread only
+        s_al[j] = al[k];
+      }
+    }
+  }
+  const float by = __ldg(sp.beam_y + i);
+  const float floor_inu = -1.0f * sp.eta * sp.minpix;
+  for (int c = 0; c < C; c++) {
+    const float freq = chfreq[c];
+    const float nudiv = freq / sp.nu_0;
+    // unrolled by two only: the transcendental functions of many pixels at
+    // once would raise the register count and lower the occupancy
+#pragma unroll 2
+    for (int k = 0; k < VPT; k++) {
+      const int j = threadIdx.x + k * blockDim.x;
+      if (j < n) {
+        // calculateInu, src/functions.cu:3939-3966
+        float inu = s_i0[j] * powf(nudiv, s_al[j]);
+        if (inu < floor_inu) inu = floor_inu;
+        // apply_beam2I, src/functions.cu:2424-2444
+        const float a =
+            attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
+        float v = inu * a * sp.fg_scale;
+        if (sp.gcf) v *= sp.gcf[(int64_t)n * i + j];  // apply_GCF, src/functions.cu:2468
+        buf[j] = make_float2(v, 0.0f);
+      }
+    }
+    __syncthreads();
+    smem_fft<VPT>(buf, sp.log2n, 1, tw);
+    float2* out = grid + (int64_t)c * sp.MN + (int64_t)n * i;
+#pragma unroll
+    for (int k = 0; k < VPT; k++) {
+      const int j = threadIdx.x + k * blockDim.x;
+      if (j < n) out[j] = buf[j];
+    }
+    __syncthreads();
+  }
 }
 
 // Pass 2 for columns j0 .. j0 + cb - 1 of grid G: column FFTs in buf
@@ -275,10 +358,13 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
   }
 }
 
-// Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate.
-__global__ void k_cols_fft(int N, int log2n, int64_t MN, int cb, const float* __restrict__ rot_u,
-                           const float* __restrict__ rot_v, const float2* __restrict__ tw_g,
-                           float2* __restrict__ grid) {
+// Pass 2: column FFTs of `cb` adjacent columns, then phase_rotate (512
+// threads, at most 64 registers each, so two blocks share an SM).
+__global__ void __launch_bounds__(512, 2) k_cols_fft(int N, int log2n, int64_t MN, int cb,
+                                                     const float* __restrict__ rot_u,
+                                                     const float* __restrict__ rot_v,
+                                                     const float2* __restrict__ tw_g,
+                                                     float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
   col_task<false, kVptLarge>(N, log2n, cb, rot_u, rot_v, tw_g, grid + (int64_t)blockIdx.y * MN, sm,
                   blockIdx.x * cb);
@@ -811,12 +897,12 @@ __global__ void __launch_bounds__(256, 2) k_objective_fused_batch(FusedBatch<Img
 
 }  // namespace
 
-// Columns per block of the column pass: 4096 / n (4K complex values of
-// shared memory, so several blocks share an SM: 2 columns at 2048^2 measured
-// 1.4x faster than 8), fewer while the launch would have under two blocks per
-// SM (small images: 256^2 runs 256 one-column blocks).
+// Columns per block of the column pass: 8192 / n (8K complex values, 64 KB
+// of shared memory: at 2048^2 four columns, so each row segment a warp reads
+// is one 32-byte sector), fewer while the launch would have under two blocks
+// per SM (small images: 256^2 runs 256 one-column blocks).
 static int cols_per_block(int n, int channels, int num_sms) {
-  int cb = 4096 / n;
+  int cb = 8192 / n;
   if (cb < 1) cb = 1;
   if (cb > 16) cb = 16;
   while (cb > 1 && (int64_t)(n / cb) * channels < 2 * (int64_t)num_sms) cb >>= 1;
@@ -858,19 +944,28 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
                              const XtSource* xs = nullptr) {
   const int n = P.N, C = (int)P.chans.size();
   const StageParams sp = stage_params(P, flag_opt, write_clip, xs);
-  const int threads = n >= 512 ? 256 : (n >= 128 ? 128 : 64);
-  const size_t sm1 = sizeof(float2) * n;
-  if (sm1 > 48 * 1024)
-    GV_CUDA(cudaFuncSetAttribute(k_rows_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
-  k_rows_fft<<<dim3(n, C), threads, sm1, P.stream>>>(sp, P.d_chfreq, d_img, P.d_mask, P.d_twiddle,
-                                                     P.d_grid);
-  GV_LAUNCH("k_rows_fft");
+  // row pass: one block of 256 threads per row, n / 256 values a thread;
+  // shared memory: the row's values and its clipped I_nu0 and alpha
+  const size_t sm1 = sizeof(float2) * n + 2 * sizeof(float) * n;
+  auto rows = [&](auto kern) -> gv_status {
+    if (sm1 > 48 * 1024)
+      GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
+    kern<<<n, 256, sm1, P.stream>>>(sp, P.d_chfreq, C, d_img, P.d_mask, P.d_twiddle, P.d_grid);
+    GV_LAUNCH("k_rows_fft");
+    return GV_OK;
+  };
+  gv_status s = n <= 512 ? rows(k_rows_fft<2>)
+                         : (n <= 1024 ? rows(k_rows_fft<4>)
+                                      : (n <= 2048 ? rows(k_rows_fft<8>) : rows(k_rows_fft<16>)));
+  if (s != GV_OK) return s;
+  // column pass: cb columns per block, 16 values a thread
   const int cb = cols_per_block(n, C, P.num_sms);
+  const int threads2 = cb * n > 4096 ? 512 : 256;
   const size_t sm2 = sizeof(float2) * (size_t)cb * n;
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-  k_cols_fft<<<dim3(n / cb, C), 256, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
-                                                      P.d_rot_v, P.d_twiddle, P.d_grid);
+  k_cols_fft<<<dim3(n / cb, C), threads2, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
+                                                           P.d_rot_v, P.d_twiddle, P.d_grid);
   GV_LAUNCH("k_cols_fft");
   return GV_OK;
 }

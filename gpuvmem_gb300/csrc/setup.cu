@@ -72,29 +72,45 @@ __global__ void __launch_bounds__(256) k_beam_moments(int64_t n, float lam,
   }
 }
 
-// k_weight_chain: reduceCPU (:353-367) of each channel's weights, one
-// thread per channel.  reduceCPU returns its running FP32 sum without the
+// k_weight_chain: reduceCPU (:353-367) of each channel's weights, one block
+// per channel.  reduceCPU returns its running FP32 sum without the
 // compensation it computes, i.e. the plain sequential FP32 sum; a
 // sequential chain reproduces it bit for bit (a parallel tree would round
-// differently).
-__global__ void k_weight_chain(int C, const int64_t* __restrict__ off,
-                               const float* __restrict__ w, float* __restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
+// differently).  Thread 0 adds a tile of 2048 weights in order from shared
+// memory while the other threads load the next tile, so the chain of
+// dependent additions, not memory latency, sets the time.
+constexpr int kChainTile = 2048;
+
+__global__ void __launch_bounds__(256) k_weight_chain(const int64_t* __restrict__ off,
+                                                      const float* __restrict__ w,
+                                                      float* __restrict__ out) {
+  __shared__ float tile[2][kChainTile];
+  const int c = blockIdx.x;
   const int64_t o = off[c], n = off[c + 1] - off[c];
-  float s = n > 0 ? w[o] : 0.0f;
-  // the additions stay in order; the loads run 32 ahead so their latency
-  // overlaps (one dependent add per value is then the critical path)
-  int64_t k = 1;
-  for (; k + 32 <= n; k += 32) {
-    float v[32];
-#pragma unroll
-    for (int t = 0; t < 32; t++) v[t] = __ldg(w + o + k + t);
-#pragma unroll
-    for (int t = 0; t < 32; t++) s = __fadd_rn(s, v[t]);
+  const int64_t ntiles = (n + kChainTile - 1) / kChainTile;
+  for (int k = threadIdx.x; k < kChainTile && k < n; k += blockDim.x) tile[0][k] = w[o + k];
+  __syncthreads();
+  float s = 0.0f;
+  for (int64_t t = 0; t < ntiles; t++) {
+    const int64_t base = t * kChainTile;
+    const int cnt = (int)(n - base < kChainTile ? n - base : kChainTile);
+    const float* cur = tile[t & 1];
+    if (threadIdx.x == 0) {
+      int k = 0;
+      if (t == 0) {
+        s = cur[0];
+        k = 1;
+      }
+      for (; k < cnt; k++) s = __fadd_rn(s, cur[k]);
+    } else {
+      const int64_t nb = base + kChainTile;
+      float* nxt = tile[(t + 1) & 1];
+      for (int64_t k = threadIdx.x - 1; k < kChainTile && nb + k < n; k += blockDim.x - 1)
+        nxt[k] = w[o + nb + k];
+    }
+    __syncthreads();
   }
-  for (; k < n; k++) s = __fadd_rn(s, w[o + k]);
-  out[c] = s;
+  if (threadIdx.x == 0) out[c] = n > 0 ? s : 0.0f;
 }
 
 __global__ void k_prepare_vis(int64_t n, int64_t off, int chan, float freq,
@@ -456,7 +472,7 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     }
     // calculateNoiseAndBeam's weight sum: reduceCPU per channel, added over
     // the channels in FP32 in order (src/functions.cu:1731-1733)
-    k_weight_chain<<<(C + 31) / 32, 32, 0, st>>>(C, d_off, d_w_in, d_wsum);
+    k_weight_chain<<<C, 256, 0, st>>>(d_off, d_w_in, d_wsum);
     GV_SETUP_CUDA(cudaGetLastError());
     {
       std::vector<float> wsum(C);
