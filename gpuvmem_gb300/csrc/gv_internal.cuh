@@ -203,10 +203,16 @@ __host__ __device__ inline float beam_coord(int k, int k0, double delta) {
 
 // attenuation(), src/functions.cu:2304-2333, with the Gaussian and Airy
 // beams of :2275-2302; float arithmetic as the reference, from the pixel's
-// offsets x, y (beam_coord).
-__device__ inline float attenuation_xy(float x, float y, float freq, float D, float pbf,
-                                       float cutoff, int pb) {
-  const float arc = sqrtf(x * x + y * y);
+// offsets x, y (beam_coord).  Split in two so a caller staging many
+// channels of one pixel takes the radius once: beam_arc (the radius, with
+// the multiply-add spelled out so every caller rounds it alike) and
+// attenuation_arc (the beam at that radius and frequency).
+__device__ __forceinline__ float beam_arc(float x, float y) {
+  return sqrtf(__fmaf_rn(x, x, __fmul_rn(y, y)));
+}
+
+__device__ inline float attenuation_arc(float arc, float freq, float D, float pbf, float cutoff,
+                                        int pb) {
   const float lambda = wavelength(freq);
   float atten;
   if (pb == GV_BEAM_GAUSSIAN) {
@@ -223,6 +229,11 @@ __device__ inline float attenuation_xy(float x, float y, float freq, float D, fl
     }
   }
   return arc <= cutoff ? atten : 0.0f;
+}
+
+__device__ inline float attenuation_xy(float x, float y, float freq, float D, float pbf,
+                                       float cutoff, int pb) {
+  return attenuation_arc(beam_arc(x, y), freq, D, pbf, cutoff, pb);
 }
 
 __device__ inline float attenuation(int i, int j, float xobs, float yobs,

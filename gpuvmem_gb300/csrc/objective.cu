@@ -72,8 +72,19 @@ __device__ __forceinline__ constexpr int brev_c(int r) {
   return o;
 }
 
+// Shared-memory position of element e of an FFT line: one float2 of padding
+// after every eight, so the first Stockham pass's writes (eight elements
+// apart across the lanes) and the second's (runs of eight, 64 apart) fall in
+// distinct banks.  A line of n elements takes fft_span(n) positions; the
+// lines of a multi-column buffer are fft_stride(n) apart (four more, so four
+// columns read row by row do not share banks either).
+__device__ __forceinline__ int fpad(int e) { return e + (e >> 3); }
+__host__ __device__ __forceinline__ int fft_span(int n) { return n + (n >> 3); }
+__host__ __device__ __forceinline__ int fft_stride(int n) { return fft_span(n) + 4; }
+
 // One Stockham autosort pass of radix R = 2^LR over `ncol` columns of length
-// n = 2^log2n in shared memory (column c at buf[c * n], natural order).
+// n = 2^log2n in shared memory (element e of column c at
+// buf[c * fft_stride(n) + fpad(e)], natural order).
 // Work item (c, j), j < n / R, reads x[j + r n/R] (r < R), multiplies by the
 // twiddles e^{2 pi i r k / (Ns R)} with k = j mod Ns (table tw[m] =
 // e^{2 pi i m / n}, read through L1), takes the R-point inverse DFT and
@@ -95,9 +106,9 @@ __device__ __forceinline__ void stockham_pass(float2* buf, int log2n, int ncol, 
     const int it = threadIdx.x + t * blockDim.x;
     if (it < items) {
       const int c = it >> lq, j = it & ((1 << lq) - 1);
-      const float2* x = buf + (c << log2n) + j;
+      const float2* x = buf + c * fft_stride(1 << log2n);
 #pragma unroll
-      for (int r = 0; r < R; r++) v[t][r] = x[r << lq];
+      for (int r = 0; r < R; r++) v[t][r] = x[fpad(j + (r << lq))];
     }
   }
   __syncthreads();
@@ -113,9 +124,10 @@ __device__ __forceinline__ void stockham_pass(float2* buf, int log2n, int ncol, 
         for (int r = 1; r < R; r++) v[t][r] = cmul(v[t][r], __ldg(tw + r * step));
       }
       dft_inv<LR>(v[t]);
-      float2* y = buf + (c << log2n) + ((j >> lNs) << (lNs + LR)) + k;
+      float2* y = buf + c * fft_stride(1 << log2n);
+      const int base = ((j >> lNs) << (lNs + LR)) + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) y[r << lNs] = v[t][brev_c<LR>(r)];
+      for (int r = 0; r < R; r++) y[fpad(base + (r << lNs))] = v[t][brev_c<LR>(r)];
     }
   }
   __syncthreads();
@@ -123,7 +135,8 @@ __device__ __forceinline__ void stockham_pass(float2* buf, int log2n, int ncol, 
 
 // In-place inverse FFT (cuFFT's CUFFT_INVERSE convention: exp(+i),
 // unnormalised) of `ncol` independent columns of length n = 2^log2n held in
-// shared memory (column c at buf[c * n]), natural order in and out: radix-8
+// shared memory (element e of column c at buf[c * fft_stride(n) + fpad(e)]),
+// natural order in and out: radix-8
 // Stockham passes, then one of radix 4 or 2.  The caller has synchronised
 // the block after filling buf; needs ncol * n <= VPT * blockDim.x and
 // n <= 2 * blockDim.x * max(1, VPT / 2).
@@ -221,19 +234,19 @@ __device__ __forceinline__ void row_task(const StageParams& sp, const float* __r
       if (i0 != i0_in) img[q] = i0;
       if (al != al_in) img[sp.MN + q] = al;
     }
-    // calculateInu, src/functions.cu:3939-3966
-    float inu = i0 * powf(nudiv, al);
+    // calculateInu, src/functions.cu:3939-3966 (powf(x, 0) is 1 exactly)
+    float inu = i0 * (al == 0.0f ? 1.0f : powf(nudiv, al));
     if (inu < floor_inu) inu = floor_inu;
     // apply_beam2I, src/functions.cu:2424-2444
     const float a = attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
     float v = inu * a * sp.fg_scale;
     if (sp.gcf) v *= sp.gcf[q];  // apply_GCF, src/functions.cu:2468
-    buf[j] = make_float2(v, 0.0f);
+    buf[fpad(j)] = make_float2(v, 0.0f);
   }
   __syncthreads();
   smem_fft<VPT>(buf, sp.log2n, 1, tw);
   float2* out = grid + (int64_t)c * sp.MN + (int64_t)n * i;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[j];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) out[j] = buf[fpad(j)];
 }
 
 // Pass 1 for row i = blockIdx.x and every channel: the row's pixels (or the
@@ -249,10 +262,12 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
                                                   const uint8_t* __restrict__ mask,
                                                   const float2* __restrict__ tw,
                                                   float2* __restrict__ grid) {
-  extern __shared__ float2 buf[];  // n values, then the row's clipped I_nu0 and alpha
+  extern __shared__ float2 buf[];  // the row (fft_span(n)), its clipped I_nu0, alpha, beam radius
   const int n = sp.N, i = blockIdx.x;
-  float* s_i0 = reinterpret_cast<float*>(buf + n);
+  float* s_i0 = reinterpret_cast<float*>(buf + fft_span(n));
   float* s_al = s_i0 + n;
+  float* s_arc = s_al + n;
+  const float by = __ldg(sp.beam_y + i);
   const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
                     sp.flag_opt};
   const bool from_xt = sp.xs.pcom != nullptr;
@@ -290,10 +305,10 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
         }
         s_i0[j] = i0[k];  // read back by this thread only
         s_al[j] = al[k];
+        s_arc[j] = beam_arc(__ldg(sp.beam_x + j), by);
       }
     }
   }
-  const float by = __ldg(sp.beam_y + i);
   const float floor_inu = -1.0f * sp.eta * sp.minpix;
   for (int c = 0; c < C; c++) {
     const float freq = chfreq[c];
@@ -304,15 +319,15 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
     for (int k = 0; k < VPT; k++) {
       const int j = threadIdx.x + k * blockDim.x;
       if (j < n) {
-        // calculateInu, src/functions.cu:3939-3966
-        float inu = s_i0[j] * powf(nudiv, s_al[j]);
+        // calculateInu, src/functions.cu:3939-3966 (powf(x, 0) is 1 exactly)
+        const float al = s_al[j];
+        float inu = s_i0[j] * (al == 0.0f ? 1.0f : powf(nudiv, al));
         if (inu < floor_inu) inu = floor_inu;
         // apply_beam2I, src/functions.cu:2424-2444
-        const float a =
-            attenuation_xy(__ldg(sp.beam_x + j), by, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
+        const float a = attenuation_arc(s_arc[j], freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
         float v = inu * a * sp.fg_scale;
         if (sp.gcf) v *= sp.gcf[(int64_t)n * i + j];  // apply_GCF, src/functions.cu:2468
-        buf[j] = make_float2(v, 0.0f);
+        buf[fpad(j)] = make_float2(v, 0.0f);
       }
     }
     __syncthreads();
@@ -321,7 +336,7 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
 #pragma unroll
     for (int k = 0; k < VPT; k++) {
       const int j = threadIdx.x + k * blockDim.x;
-      if (j < n) out[j] = buf[j];
+      if (j < n) out[j] = buf[fpad(j)];
     }
     __syncthreads();
   }
@@ -337,15 +352,16 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
                                          const float* __restrict__ rot_v, const float2* tw,
                                          float2* __restrict__ G, float2* buf, int j0) {
   const int n = N;
+  const int lcb = __ffs(cb) - 1;  // cb is a power of two
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
-    const int r = idx / cb, cc = idx - r * cb;
+    const int r = idx >> lcb, cc = idx & (cb - 1);
     const float2* src = G + (int64_t)n * r + j0 + cc;
-    buf[cc * n + r] = kL2Loads ? __ldcg(src) : *src;
+    buf[cc * fft_stride(n) + fpad(r)] = kL2Loads ? __ldcg(src) : *src;
   }
   __syncthreads();
   smem_fft<VPT>(buf, log2n, cb, tw);
   for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
-    const int r = idx / cb, cc = idx - r * cb;
+    const int r = idx >> lcb, cc = idx & (cb - 1);
     const int j = j0 + cc;
     // u = xphs / n * (j or j - n), v likewise for the row, in FP64 rounded
     // to float (the tables hold them)
@@ -354,7 +370,7 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
     const float phase = -2.0f * (u + v);
     float s, co;
     sincospif(phase, &s, &co);
-    G[(int64_t)n * r + j] = cmul(buf[cc * n + r], make_float2(co, s));
+    G[(int64_t)n * r + j] = cmul(buf[cc * fft_stride(n) + fpad(r)], make_float2(co, s));
   }
 }
 
@@ -792,7 +808,7 @@ template <class Img>
 __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
   extern __shared__ float2 sm[];
   const int n = f.sp.N;
-  float2* buf = sm;  // n * cb values
+  float2* buf = sm;  // cb columns, fft_stride(n) apart
   const float2* tw = f.tw;
   float2* grid = const_cast<float2*>(f.da.grid);
   // A: rows of every channel, then the prior-value tasks
@@ -945,8 +961,8 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   const int n = P.N, C = (int)P.chans.size();
   const StageParams sp = stage_params(P, flag_opt, write_clip, xs);
   // row pass: one block of 256 threads per row, n / 256 values a thread;
-  // shared memory: the row's values and its clipped I_nu0 and alpha
-  const size_t sm1 = sizeof(float2) * n + 2 * sizeof(float) * n;
+  // shared memory: the row's values, its clipped I_nu0 and alpha, beam radii
+  const size_t sm1 = sizeof(float2) * fft_span(n) + 3 * sizeof(float) * n;
   auto rows = [&](auto kern) -> gv_status {
     if (sm1 > 48 * 1024)
       GV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
@@ -961,7 +977,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   // column pass: cb columns per block, 16 values a thread
   const int cb = cols_per_block(n, C, P.num_sms);
   const int threads2 = cb * n > 4096 ? 512 : 256;
-  const size_t sm2 = sizeof(float2) * (size_t)cb * n;
+  const size_t sm2 = sizeof(float2) * (size_t)cb * fft_stride(n);
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
   k_cols_fft<<<dim3(n / cb, C), threads2, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
@@ -1050,7 +1066,7 @@ static gv_status fused_launch(Problem& P, float* d_img, int flag_opt, bool store
                               const PriorSet<Img>& ps) {
   const int n = P.N, C = (int)P.chans.size();
   const FusedArgs<Img> f = fused_args(P, d_img, flag_opt, store_res, xs, term_out, zero_terms, ps);
-  const size_t smem = sizeof(float2) * (size_t)(n * f.cb);
+  const size_t smem = sizeof(float2) * (size_t)f.cb * fft_stride(n);
   int& blocks = P.fused_blocks[ImgKind<Img>::k];
   if (blocks == 0) {
     // every block must be resident at once: at most the occupancy bound,
@@ -1213,7 +1229,7 @@ gv_status batch_objective_launch(int np, const void* d_args, const int* d_off, i
                                  cudaStream_t st) {
   FusedBatch<ClipImage> fb{static_cast<const FusedArgs<ClipImage>*>(d_args), d_off, np, 1, d_bar,
                            d_err};
-  const size_t smem = sizeof(float2) * (size_t)max_n;
+  const size_t smem = sizeof(float2) * (size_t)fft_stride(max_n);
   int occ = 0;
   GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_objective_fused_batch<ClipImage>,
                                                         256, smem));
