@@ -461,28 +461,55 @@ __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, 
   const int N = a.N;
   const int nm1 = N - 1;
   CompSum acc;
-  for (int64_t k = b * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
-       k += (int64_t)nb * blockDim.x) {
-    const float4 d = __ldcs(a.deg + rg.off + k);
-    const float2 o = __ldcs(a.vo + rg.off + k);
-    const uint32_t cell = __float_as_uint(d.x);
-    const int i1 = cell & 0xffff, j1 = cell >> 16;
-    const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
-    const float2 v11 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i1) : __ldg(G + (int64_t)N * j1 + i1);
-    const float2 v12 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i1) : __ldg(G + (int64_t)N * j2 + i1);
-    const float2 v21 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i2) : __ldg(G + (int64_t)N * j1 + i2);
-    const float2 v22 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i2) : __ldg(G + (int64_t)N * j2 + i2);
-    const float du = d.y, dv = d.z;
-    const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
-    const float w21 = du * (1.0f - dv), w22 = du * dv;
-    const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
-    const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
-    const float rr = o.x - mr, ri = o.y - mi;
-    acc.add(d.w * (rr * rr + ri * ri));
-    if (a.store) {
-      const float2 cv = make_float2(d.w * rr, d.w * ri);
-      __stcs(a.cvr + rg.off + k, cv);
-      mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
+  // four of the thread's visibilities at a time: their streams and grid
+  // gathers are all loaded before any is used (the residual stores could
+  // alias them as far as the compiler knows), then added in order
+  constexpr int kU = 4;
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  for (int64_t k0 = b * (int64_t)blockDim.x + threadIdx.x; k0 < rg.ngrid; k0 += kU * stride) {
+    float4 d[kU];
+    float2 o[kU], v11[kU], v12[kU], v21[kU], v22[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t k = k0 + u * stride;
+      if (k < rg.ngrid) {
+        d[u] = __ldcs(a.deg + rg.off + k);
+        o[u] = __ldcs(a.vo + rg.off + k);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (k0 + u * stride < rg.ngrid) {
+        const uint32_t cell = __float_as_uint(d[u].x);
+        const int i1 = cell & 0xffff, j1 = cell >> 16;
+        const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
+        const float2* g11 = G + (int64_t)N * j1 + i1;
+        const float2* g12 = G + (int64_t)N * j2 + i1;
+        const float2* g21 = G + (int64_t)N * j1 + i2;
+        const float2* g22 = G + (int64_t)N * j2 + i2;
+        v11[u] = kL2Loads ? __ldcg(g11) : __ldg(g11);
+        v12[u] = kL2Loads ? __ldcg(g12) : __ldg(g12);
+        v21[u] = kL2Loads ? __ldcg(g21) : __ldg(g21);
+        v22[u] = kL2Loads ? __ldcg(g22) : __ldg(g22);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t k = k0 + u * stride;
+      if (k < rg.ngrid) {
+        const float du = d[u].y, dv = d[u].z;
+        const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
+        const float w21 = du * (1.0f - dv), w22 = du * dv;
+        const float mr = w11 * v11[u].x + w12 * v12[u].x + w21 * v21[u].x + w22 * v22[u].x;
+        const float mi = w11 * v11[u].y + w12 * v12[u].y + w21 * v21[u].y + w22 * v22[u].y;
+        const float rr = o[u].x - mr, ri = o[u].y - mi;
+        acc.add(d[u].w * (rr * rr + ri * ri));
+        if (a.store) {
+          const float2 cv = make_float2(d[u].w * rr, d[u].w * ri);
+          __stcs(a.cvr + rg.off + k, cv);
+          mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
+        }
+      }
     }
   }
   if (a.store) {
@@ -505,7 +532,7 @@ __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, 
 
 // Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
 // block to finish adds the partials into the chi2 scalar.
-__global__ void __launch_bounds__(256) k_degrid(DegridArgs a) {
+__global__ void __launch_bounds__(256, 3) k_degrid(DegridArgs a) {
   degrid_task<false>(a, blockIdx.x, gridDim.x, blockIdx.y, gridDim.y);
 }
 
