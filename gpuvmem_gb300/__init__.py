@@ -137,6 +137,7 @@ def lib():
         "gv_optimize": [vp, C.POINTER(OptDesc), vp, C.POINTER(OptReport)],
         "gv_optimize_until": [vp, C.POINTER(OptDesc), vp, f64, i32, C.POINTER(OptReport)],
         "gv_set_iteration": [vp, i32],
+        "gv_linmin": [vp, vp, vp, i32, i32, C.POINTER(C.c_float), C.POINTER(C.c_int64)],
         "gv_dirty_image": [vp, vp],
         "gv_psf_image": [vp, vp],
         "gv_residuals": [vp, f32p],
@@ -390,6 +391,16 @@ class Problem:
         check(lib().gv_optimize_until(self.h, C.byref(o), _ptr(img), float(f_target),
                                       int(bool(priors_from_start)), C.byref(rep)))
         return rep
+
+    def linmin(self, p, xi, flag_opt=0, positivity=True):
+        """linmin (src/linmin.cu:52-110): minimise the objective along xi
+        from p; p and xi are updated in place as newP leaves them.  Returns
+        (fret, objective evaluations)."""
+        fret = C.c_float()
+        evals = C.c_int64()
+        check(lib().gv_linmin(self.h, _ptr(p), _ptr(xi), flag_opt, int(bool(positivity)),
+                              C.byref(fret), C.byref(evals)))
+        return fret.value, evals.value
 
     def error_images(self, img):
         """calculateErrors: (2, N, M) error images of the solution img."""

@@ -305,6 +305,23 @@ gv_status gv_optimize(gv_problem* p, const gv_opt_desc* opt, float* d_img, gv_op
   return gv::check_device_error(p->P);
 }
 
+gv_status gv_linmin(gv_problem* p, float* d_p, float* d_xi, int32_t flag_opt,
+                    int32_t positivity, float* fret, int64_t* evals) {
+  GV_CHECK_PROBLEM(p);
+  if (!d_p || !d_xi || !fret) { gv::set_error("null image, direction or output"); return GV_ERR_INVALID; }
+  gv_opt_desc o;
+  std::memset(&o, 0, sizeof(o));
+  o.kind = GV_OPT_FRPRMN;
+  o.ftol = 1e-12f;
+  o.gtol = 1e-12f;
+  o.K = 1;
+  o.flag = flag_opt;
+  o.positivity = positivity ? 1 : 0;
+  gv_status s = gv::linmin(p->P, o, d_p, d_xi, fret, evals);
+  if (s != GV_OK) return s;
+  return gv::check_device_error(p->P);
+}
+
 gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img, double f_target,
                             int32_t priors_from_start, gv_opt_report* report) {
   GV_CHECK_PROBLEM(p);

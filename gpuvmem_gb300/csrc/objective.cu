@@ -25,6 +25,7 @@
 #include <cstring>
 
 #include "gv_internal.cuh"
+#include "ls_core.cuh"
 
 namespace gv {
 
@@ -212,7 +213,7 @@ __device__ __forceinline__ void row_task(const StageParams& sp, const float* __r
                     sp.flag_opt};
   const bool writer = sp.write_clip && c == 0;
   const bool from_xt = sp.xs.pcom != nullptr;
-  const float x = from_xt ? *sp.xs.x_dev : 0.0f;
+  const float x = from_xt ? __ldcg(sp.xs.x_dev) : 0.0f;
   const float by = __ldg(sp.beam_y + i);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const int64_t q = (int64_t)n * i + j;
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
   const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
                     sp.flag_opt};
   const bool from_xt = sp.xs.pcom != nullptr;
-  const float x = from_xt ? *sp.xs.x_dev : 0.0f;
+  const float x = from_xt ? __ldcg(sp.xs.x_dev) : 0.0f;
   {
     float i0[VPT], al[VPT];
 #pragma unroll
@@ -451,65 +452,38 @@ struct DegridArgs {
 // Pass 3 for block b of nb of channel c: vis_mod + residual + chi2Vector
 // over the block's share of the cell-sorted visibilities and the block's
 // FP64 partial; the last of the nb * C blocks to finish adds the partials
-// into the chi2 scalar.  kL2Loads: read the grid from L2 (written earlier in
-// the same kernel by other blocks).
+// into the chi2 scalar (and returns true).  kL2Loads: read the grid from L2
+// (written earlier in the same kernel by other blocks).
 template <bool kL2Loads>
-__device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
+__device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
   float mx = 0.0f;
   const ChanRange rg = a.ranges[c];
   const float2* __restrict__ G = a.grid + (int64_t)c * a.MN;
   const int N = a.N;
   const int nm1 = N - 1;
   CompSum acc;
-  // four of the thread's visibilities at a time: their streams and grid
-  // gathers are all loaded before any is used (the residual stores could
-  // alias them as far as the compiler knows), then added in order
-  constexpr int kU = 4;
-  const int64_t stride = (int64_t)nb * blockDim.x;
-  for (int64_t k0 = b * (int64_t)blockDim.x + threadIdx.x; k0 < rg.ngrid; k0 += kU * stride) {
-    float4 d[kU];
-    float2 o[kU], v11[kU], v12[kU], v21[kU], v22[kU];
-#pragma unroll
-    for (int u = 0; u < kU; u++) {
-      const int64_t k = k0 + u * stride;
-      if (k < rg.ngrid) {
-        d[u] = __ldcs(a.deg + rg.off + k);
-        o[u] = __ldcs(a.vo + rg.off + k);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kU; u++) {
-      if (k0 + u * stride < rg.ngrid) {
-        const uint32_t cell = __float_as_uint(d[u].x);
-        const int i1 = cell & 0xffff, j1 = cell >> 16;
-        const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
-        const float2* g11 = G + (int64_t)N * j1 + i1;
-        const float2* g12 = G + (int64_t)N * j2 + i1;
-        const float2* g21 = G + (int64_t)N * j1 + i2;
-        const float2* g22 = G + (int64_t)N * j2 + i2;
-        v11[u] = kL2Loads ? __ldcg(g11) : __ldg(g11);
-        v12[u] = kL2Loads ? __ldcg(g12) : __ldg(g12);
-        v21[u] = kL2Loads ? __ldcg(g21) : __ldg(g21);
-        v22[u] = kL2Loads ? __ldcg(g22) : __ldg(g22);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kU; u++) {
-      const int64_t k = k0 + u * stride;
-      if (k < rg.ngrid) {
-        const float du = d[u].y, dv = d[u].z;
-        const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
-        const float w21 = du * (1.0f - dv), w22 = du * dv;
-        const float mr = w11 * v11[u].x + w12 * v12[u].x + w21 * v21[u].x + w22 * v22[u].x;
-        const float mi = w11 * v11[u].y + w12 * v12[u].y + w21 * v21[u].y + w22 * v22[u].y;
-        const float rr = o[u].x - mr, ri = o[u].y - mi;
-        acc.add(d[u].w * (rr * rr + ri * ri));
-        if (a.store) {
-          const float2 cv = make_float2(d[u].w * rr, d[u].w * ri);
-          __stcs(a.cvr + rg.off + k, cv);
-          mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
-        }
-      }
+  for (int64_t k = b * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
+       k += (int64_t)nb * blockDim.x) {
+    const float4 d = __ldcs(a.deg + rg.off + k);
+    const float2 o = __ldcs(a.vo + rg.off + k);
+    const uint32_t cell = __float_as_uint(d.x);
+    const int i1 = cell & 0xffff, j1 = cell >> 16;
+    const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
+    const float2 v11 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i1) : __ldg(G + (int64_t)N * j1 + i1);
+    const float2 v12 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i1) : __ldg(G + (int64_t)N * j2 + i1);
+    const float2 v21 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i2) : __ldg(G + (int64_t)N * j1 + i2);
+    const float2 v22 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i2) : __ldg(G + (int64_t)N * j2 + i2);
+    const float du = d.y, dv = d.z;
+    const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
+    const float w21 = du * (1.0f - dv), w22 = du * dv;
+    const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
+    const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
+    const float rr = o.x - mr, ri = o.y - mi;
+    acc.add(d.w * (rr * rr + ri * ri));
+    if (a.store) {
+      const float2 cv = make_float2(d.w * rr, d.w * ri);
+      __stcs(a.cvr + rg.off + k, cv);
+      mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
     }
   }
   if (a.store) {
@@ -527,12 +501,14 @@ __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, 
       for (int t = 0; t < 32; t++)
         if (a.zero_terms & (1u << t)) a.term_slots[t] = 0.0;
     }
+    return true;
   }
+  return false;
 }
 
 // Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
 // block to finish adds the partials into the chi2 scalar.
-__global__ void __launch_bounds__(256, 3) k_degrid(DegridArgs a) {
+__global__ void __launch_bounds__(256) k_degrid(DegridArgs a) {
   degrid_task<false>(a, blockIdx.x, gridDim.x, blockIdx.y, gridDim.y);
 }
 
@@ -668,7 +644,7 @@ struct XtImage {
   ClipRule cr;
   int plane;
   float x;
-  __device__ void bind() { x = *xs.x_dev; }
+  __device__ void bind() { x = __ldcg(xs.x_dev); }
   __device__ __forceinline__ float operator[](int64_t q) const {
     float i0, al;
     xt_pixel(xs, x, MN, q, i0, al);
@@ -811,6 +787,43 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* err) {
   return ok != 0;
 }
 
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier number k (0, 1, 2, ...) of a cooperative launch whose
+// counters start at zero: arrivals go to a monotone counter (no reset
+// between barriers), and the last arrival of barrier k publishes epoch k + 1
+// on a word of its own, which the other blocks poll.  Bounded like
+// grid_barrier (1 s, error bit 16, false in every thread of the block).
+__device__ bool grid_sync(uint32_t* cnt, uint32_t* epoch, uint32_t k, uint32_t* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const uint32_t prev = atomicAdd(cnt, 1u);
+    int good = 1;
+    if (prev == (k + 1) * gridDim.x - 1) {
+      __threadfence();
+      st_release_gpu(epoch, k + 1);
+    } else {
+      const uint64_t t0 = global_ns();
+      uint32_t spins = 0;
+      while (ld_acquire_gpu(epoch) < k + 1) {
+        __nanosleep(20);
+        if ((++spins & 63u) == 0u && global_ns() - t0 > 1000000000ull) {
+          atomicOr(err, 16u);
+          good = 0;
+          break;
+        }
+      }
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 template <class Img>
 struct FusedArgs {
   StageParams sp;
@@ -862,6 +875,99 @@ __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
   // C: degridding and chi2
   for (int t = blockIdx.x; t < f.nb_deg * f.C; t += gridDim.x)
     degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C);
+}
+
+// ---- small images: a whole line search in one cooperative launch --------
+//
+// linmin's bracket + Brent search (src/linmin.cu:52-110, the state machine
+// of ls_core.cuh) with every objective evaluation as k_objective_fused's
+// phases, all in one cooperative launch.  Per evaluation, at
+// xt = pcom + x_req xicom:
+//   A  row tasks, and prior-value tasks on the blocks the rows leave free;
+//      grid barrier;
+//   B  column tasks and the remaining prior-value tasks; grid barrier;
+//   C  degridding tasks; the block that sums chi2 also takes the search's
+//      step (the next x_req, or the end); grid barrier.
+// The tasks are the separate launches' blocks (same block size, same partial
+// slots, same order of the final sums), so each evaluation, and with it the
+// search, is bit-identical to the graph loop of separate launches.  The loop
+// ends when the search does (at its evaluation cap at the latest) or when a
+// grid barrier times out.
+
+struct LinminArgs {
+  FusedArgs<XtImage> f;
+  int prior_a;       // prior-value tasks run in phase A (the rest in phase B)
+  LsState* ls;
+  double* scal;
+  uint32_t* stop;    // set to 1 by the stepping block when the search is over
+  uint32_t* bar_count;  // grid_sync counters (zero at the launch)
+  uint32_t* bar_epoch;
+};
+
+// the search's step, out of line: one thread once per evaluation, so its
+// state copy and branches do not weigh on the kernel's registers
+__device__ __noinline__ uint32_t linmin_step(LsState* ls, double* scal) {
+  return ls::ls_step(ls, scal) ? 0u : 1u;
+}
+
+// The phases of one evaluation, out of line so that each is register-
+// allocated on its own.
+__device__ __noinline__ void linmin_phase_a(const LinminArgs& a, float2* sm) {
+  const FusedArgs<XtImage>& f = a.f;
+  const int n = f.sp.N, nrow = n * f.C;
+  for (int t = blockIdx.x; t < nrow + a.prior_a; t += gridDim.x) {
+    if (t < nrow) {
+      row_task<kVptSmall>(f.sp, f.chfreq, f.img, f.mask, f.tw, const_cast<float2*>(f.da.grid), sm,
+                          t % n, t / n);
+    } else {
+      const int u = t - nrow;
+      prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __noinline__ void linmin_phase_b(const LinminArgs& a, float2* sm) {
+  const FusedArgs<XtImage>& f = a.f;
+  const int n = f.sp.N, ncg = n / f.cb, ncol = ncg * f.C;
+  const int nprior = f.nb_prior * f.ps.n;
+  for (int t = blockIdx.x; t < ncol + nprior - a.prior_a; t += gridDim.x) {
+    if (t < ncol) {
+      col_task<true, kVptSmall>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, f.tw,
+                                const_cast<float2*>(f.da.grid) + (int64_t)(t / ncg) * f.sp.MN, sm,
+                                (t % ncg) * f.cb);
+    } else {
+      const int u = a.prior_a + t - ncol;
+      prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __noinline__ void linmin_phase_c(const LinminArgs& a) {
+  const FusedArgs<XtImage>& f = a.f;
+  for (int t = blockIdx.x; t < f.nb_deg * f.C; t += gridDim.x) {
+    if (degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C) && threadIdx.x == 0) {
+      *a.stop = linmin_step(a.ls, a.scal);
+      __threadfence();
+    }
+  }
+}
+
+// kBps: the blocks per SM the registers are budgeted for (2: 128 a thread,
+// 3: 80, with the degridding phase spilling a little)
+template <int kBps>
+__global__ void __launch_bounds__(256, kBps) k_linmin_fused(const __grid_constant__ LinminArgs a) {
+  extern __shared__ float2 sm[];
+  for (uint32_t k = 0;; k += 3) {
+    linmin_phase_a(a, sm);  // rows at the search's point, prior values
+    if (!grid_sync(a.bar_count, a.bar_epoch, k, a.f.err)) return;
+    linmin_phase_b(a, sm);  // columns, the remaining prior values
+    if (!grid_sync(a.bar_count, a.bar_epoch, k + 1, a.f.err)) return;
+    linmin_phase_c(a);      // degridding and chi2, then the search's step
+    if (!grid_sync(a.bar_count, a.bar_epoch, k + 2, a.f.err)) return;
+    if (__ldcg(a.stop) != 0u) return;
+  }
 }
 
 // ---- batches: the objectives of several problems in one cooperative launch
@@ -1367,6 +1473,85 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
   gv_status s = chi2_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero);
   if (s != GV_OK) return s;
   if (ps.n > 0) GV_CUDA(cudaStreamWaitEvent(P.stream, join, 0));
+  return GV_OK;
+}
+
+// Images up to 512 x 512 with k_degrid's default block size (the fused tasks
+// reproduce its 256-thread blocks), no caller running several problems at
+// once, and GV_LS_FUSED not 0 at creation.
+bool linmin_fused_ok(const Problem& P) {
+  return P.ls_fused && P.fused_off == 0 && P.N <= 512 && P.degrid_threads == 256;
+}
+
+gv_status linmin_fused_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
+                              LsState* ls) {
+  // the terms as ls_objective_launch arranges them
+  int ichi2 = -1;
+  uint32_t zero = 0u;
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    if (P.terms[t].kind == GV_FI_CHI2) {
+      if (ichi2 < 0) ichi2 = (int)t;
+    } else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) {
+      zero |= 1u << t;
+    }
+  }
+  if (ichi2 < 0) {
+    set_error("a line-search evaluation needs the Chi2 term");
+    return GV_ERR_UNSUPPORTED;
+  }
+  PriorSet<XtImage> ps{};
+  const int64_t MN = (int64_t)P.M * P.N;
+  const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
+                    flag_opt};
+  for (size_t t = 0; t < P.terms.size(); t++) {
+    const Term& tm = P.terms[t];
+    if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
+    const int k = ps.n++;
+    ps.pp[k] = prior_params(P, tm);
+    ps.img[k] = XtImage{xs, P.d_mask, MN, cr, tm.image_index, 0.0f};
+    ps.part[k] = prior_part(P, (int)t);
+    ps.out[k] = P.d_scal + kSlotTerm0 + t;
+  }
+  const int n = P.N, C = (int)P.chans.size();
+  LinminArgs a{};
+  a.f = fused_args(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero, ps);
+  a.ls = ls;
+  a.scal = P.d_scal;
+  a.stop = P.d_flags + kFlagLsStop;
+  a.bar_count = P.d_flags + kFlagLsBarCount;
+  a.bar_epoch = P.d_flags + kFlagLsBarEpoch;
+  const size_t smem = sizeof(float2) * (size_t)a.f.cb * fft_stride(n);
+  const int bps = P.ls_blocks_per_sm == 3 ? 3 : 2;
+  auto kern = bps == 3 ? k_linmin_fused<3> : k_linmin_fused<2>;
+  if (P.linmin_blocks == 0) {
+    // every block resident at once: the occupancy bound, at most bps blocks
+    // per SM, and no more than the largest phase has tasks
+    int occ = 0;
+    GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
+    if (occ < 1) {
+      set_error("k_linmin_fused does not fit on an SM");
+      return GV_ERR_UNSUPPORTED;
+    }
+    const int tasks = std::max(n * C + a.f.nb_prior * kMaxTerms, a.f.nb_deg * C);
+    P.linmin_blocks = std::max(1, std::min(P.num_sms * std::min(occ, bps), tasks));
+  }
+  const int blocks = P.linmin_blocks;
+  const int nprior = a.f.nb_prior * ps.n;
+  a.prior_a = std::min(nprior, std::max(0, blocks - n * C));
+  GV_CUDA(cudaMemsetAsync(a.bar_count, 0,
+                          sizeof(uint32_t) * (kFlagLsBarEpoch - kFlagLsBarCount + 1), P.stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = P.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GV_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  GV_LAUNCH("k_linmin_fused");
   return GV_OK;
 }
 

@@ -250,6 +250,19 @@ gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img,
                             double f_target, int32_t priors_from_start,
                             gv_opt_report* report);
 
+/* linmin (src/linmin.cu:52-110): the objective minimised along d_xi from
+ * d_p by the bracketing (src/mnbrak.cu:44-98) and Brent (src/brent.cu:43-121,
+ * TOL 1e-7) search that gv_optimize's iterations run, then newP
+ * (src/functions.cu:2760-2777): d_xi = xmin d_xi and d_p = d_p + d_xi, plane 0
+ * floored at -eta*MINPIX with positivity (its d_xi then 0).  *fret is the
+ * objective at the minimum and *evals (may be null) the evaluations the search
+ * took.  d_p and d_xi are device images (2 x M x N floats).  The priors count
+ * as Fi::iteration (gv_set_iteration) says.  Images up to 512 x 512 run the
+ * whole search as one cooperative launch (GV_LS_FUSED=0 at creation: a CUDA
+ * graph loop of separate launches); results are identical either way. */
+gv_status gv_linmin(gv_problem* p, float* d_p, float* d_xi, int32_t flag_opt,
+                    int32_t positivity, float* fret, int64_t* evals);
+
 /* Fi::setIteration(iter) on every term: iter > 0 makes the priors count in
  * the next gv_objective (the reference sets it only inside calcGradient,
  * include/classes/objectivefunction.cuh:39). */

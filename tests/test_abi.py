@@ -62,6 +62,7 @@ def test_null_handles_are_rejected_without_gpu():
         lambda: L.gv_evaluate(None, None, None, 0, 0, ctypes.byref(f), None),
         lambda: L.gv_dchi2(None, None, 0, None),
         lambda: L.gv_problem_set_graphs(None, 1),
+        lambda: L.gv_linmin(None, None, None, 0, 1, ctypes.byref(ctypes.c_float()), None),
     ]
     for call in calls:
         assert call() == 1
