@@ -24,12 +24,16 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "gv_internal.cuh"
 #include "ls_core.cuh"
 
 namespace gv {
 
 namespace {
+
+namespace cg = cooperative_groups;
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -197,6 +201,20 @@ struct StageParams {
   XtSource xs;       // xs.pcom set: the image is xt = pcom + x xicom (written back)
 };
 
+// One staged pixel of a channel: calculateInu (src/functions.cu:3939-3966;
+// powf(x, 0) is 1 exactly) floored at -eta * MINPIX, apply_beam2I
+// (src/functions.cu:2424-2444) at beam radius arc, fg_scale, and apply_GCF
+// (src/functions.cu:2468) when a correction is set.
+__device__ __forceinline__ float stage_value(const StageParams& sp, float i0, float al, float arc,
+                                             float freq, float nudiv, float floor_inu, int64_t q) {
+  float inu = i0 * (al == 0.0f ? 1.0f : powf(nudiv, al));
+  if (inu < floor_inu) inu = floor_inu;
+  const float a = attenuation_arc(arc, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
+  float v = inu * a * sp.fg_scale;
+  if (sp.gcf) v *= sp.gcf[q];
+  return v;
+}
+
 // Pass 1 for row i of channel c: stage I_nu * A * fg_scale into buf (shared
 // memory, n float2) and FFT the row with the twiddles tw (shared memory);
 // the row goes to grid.  Every thread of the block takes part.
@@ -320,15 +338,9 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
     for (int k = 0; k < VPT; k++) {
       const int j = threadIdx.x + k * blockDim.x;
       if (j < n) {
-        // calculateInu, src/functions.cu:3939-3966 (powf(x, 0) is 1 exactly)
-        const float al = s_al[j];
-        float inu = s_i0[j] * (al == 0.0f ? 1.0f : powf(nudiv, al));
-        if (inu < floor_inu) inu = floor_inu;
-        // apply_beam2I, src/functions.cu:2424-2444
-        const float a = attenuation_arc(s_arc[j], freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
-        float v = inu * a * sp.fg_scale;
-        if (sp.gcf) v *= sp.gcf[(int64_t)n * i + j];  // apply_GCF, src/functions.cu:2468
-        buf[fpad(j)] = make_float2(v, 0.0f);
+        buf[fpad(j)] = make_float2(
+            stage_value(sp, s_i0[j], s_al[j], s_arc[j], freq, nudiv, floor_inu, (int64_t)n * i + j),
+            0.0f);
       }
     }
     __syncthreads();
@@ -341,6 +353,16 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
     }
     __syncthreads();
   }
+}
+
+// phase_rotate (src/functions.cu:2483-2518) of one grid value in the
+// reference's float arithmetic: u, v are x_phs / n * (j or j - n) and the row
+// equivalent, in FP64 rounded to float (the tables hold them)
+__device__ __forceinline__ float2 phase_rotated(float2 g, float u, float v) {
+  const float phase = -2.0f * (u + v);
+  float s, co;
+  sincospif(phase, &s, &co);
+  return cmul(g, make_float2(co, s));
 }
 
 // Pass 2 for columns j0 .. j0 + cb - 1 of grid G: column FFTs in buf
@@ -366,12 +388,8 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
     const int j = j0 + cc;
     // u = xphs / n * (j or j - n), v likewise for the row, in FP64 rounded
     // to float (the tables hold them)
-    const float u = __ldg(rot_u + j);
-    const float v = __ldg(rot_v + r);
-    const float phase = -2.0f * (u + v);
-    float s, co;
-    sincospif(phase, &s, &co);
-    G[(int64_t)n * r + j] = cmul(buf[cc * fft_stride(n) + fpad(r)], make_float2(co, s));
+    G[(int64_t)n * r + j] = phase_rotated(buf[cc * fft_stride(n) + fpad(r)], __ldg(rot_u + j),
+                                          __ldg(rot_v + r));
   }
 }
 
@@ -449,6 +467,27 @@ struct DegridArgs {
   double* __restrict__ term_slots;
 };
 
+// vis_mod (src/functions.cu:2557-2609): bilinear interpolation of the grid
+// at the visibility's fractional cell offsets (d.y, d.z) from the four cell
+// values v11 (row j1, column i1), v12 (j2, i1), v21 (j1, i2), v22 (j2, i2);
+// the residual Vo - Vm (src/functions.cu:2663) goes to rr, ri.  Every
+// degridding path calls this, so they round alike.
+__device__ __forceinline__ void vis_residual(const float4& d, float2 o, float2 v11, float2 v12,
+                                             float2 v21, float2 v22, float& rr, float& ri) {
+  const float du = d.y, dv = d.z;
+  const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
+  const float w21 = du * (1.0f - dv), w22 = du * dv;
+  const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
+  const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
+  rr = o.x - mr;
+  ri = o.y - mi;
+}
+
+// chi2Vector (src/functions.cu:2867): w |Vr|^2
+__device__ __forceinline__ float chi2_term(float w, float rr, float ri) {
+  return w * (rr * rr + ri * ri);
+}
+
 // Pass 3 for block b of nb of channel c: vis_mod + residual + chi2Vector
 // over the block's share of the cell-sorted visibilities and the block's
 // FP64 partial; the last of the nb * C blocks to finish adds the partials
@@ -473,13 +512,9 @@ __device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, 
     const float2 v12 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i1) : __ldg(G + (int64_t)N * j2 + i1);
     const float2 v21 = kL2Loads ? __ldcg(G + (int64_t)N * j1 + i2) : __ldg(G + (int64_t)N * j1 + i2);
     const float2 v22 = kL2Loads ? __ldcg(G + (int64_t)N * j2 + i2) : __ldg(G + (int64_t)N * j2 + i2);
-    const float du = d.y, dv = d.z;
-    const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
-    const float w21 = du * (1.0f - dv), w22 = du * dv;
-    const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
-    const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
-    const float rr = o.x - mr, ri = o.y - mi;
-    acc.add(d.w * (rr * rr + ri * ri));
+    float rr, ri;
+    vis_residual(d, o, v11, v12, v21, v22, rr, ri);
+    acc.add(chi2_term(d.w, rr, ri));
     if (a.store) {
       const float2 cv = make_float2(d.w * rr, d.w * ri);
       __stcs(a.cvr + rg.off + k, cv);
@@ -787,43 +822,6 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* err) {
   return ok != 0;
 }
 
-__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
-}
-
-// Grid-wide barrier number k (0, 1, 2, ...) of a cooperative launch whose
-// counters start at zero: arrivals go to a monotone counter (no reset
-// between barriers), and the last arrival of barrier k publishes epoch k + 1
-// on a word of its own, which the other blocks poll.  Bounded like
-// grid_barrier (1 s, error bit 16, false in every thread of the block).
-__device__ bool grid_sync(uint32_t* cnt, uint32_t* epoch, uint32_t k, uint32_t* err) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const uint32_t prev = atomicAdd(cnt, 1u);
-    int good = 1;
-    if (prev == (k + 1) * gridDim.x - 1) {
-      __threadfence();
-      st_release_gpu(epoch, k + 1);
-    } else {
-      const uint64_t t0 = global_ns();
-      uint32_t spins = 0;
-      while (ld_acquire_gpu(epoch) < k + 1) {
-        __nanosleep(20);
-        if ((++spins & 63u) == 0u && global_ns() - t0 > 1000000000ull) {
-          atomicOr(err, 16u);
-          good = 0;
-          break;
-        }
-      }
-    }
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
 template <class Img>
 struct FusedArgs {
   StageParams sp;
@@ -877,32 +875,241 @@ __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
     degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C);
 }
 
-// ---- small images: a whole line search in one cooperative launch --------
+// ---- small single-channel images: a whole line search in one cluster -----
 //
-// linmin's bracket + Brent search (src/linmin.cu:52-110, the state machine
-// of ls_core.cuh) with every objective evaluation as k_objective_fused's
-// phases, all in one cooperative launch.  Per evaluation, at
-// xt = pcom + x_req xicom:
-//   A  row tasks, and prior-value tasks on the blocks the rows leave free;
-//      grid barrier;
-//   B  column tasks and the remaining prior-value tasks; grid barrier;
-//   C  degridding tasks; the block that sums chi2 also takes the search's
-//      step (the next x_req, or the end); grid barrier.
-// The tasks are the separate launches' blocks (same block size, same partial
-// slots, same order of the final sums), so each evaluation, and with it the
-// search, is bit-identical to the graph loop of separate launches.  The loop
-// ends when the search does (at its evaluation cap at the latest) or when a
-// grid barrier times out.
+// linmin's search (src/linmin.cu:52-110, the state machine of ls_core.cuh)
+// with every objective evaluation done by one thread-block cluster that
+// keeps the channel's grid on chip.  CTA r of the kCtas stages and
+// row-transforms image rows [r R, r R + R) (R = N / kCtas) into its shared
+// memory; gathers columns [r R, r R + R) of the row transforms from every
+// CTA's shared memory (distributed shared memory), column-transforms and
+// phase-rotates them in place; and the degridding reads each visibility's
+// four cells from the CTAs that hold their columns.  Cluster barriers (in
+// hardware) separate the phases, so the search is one launch with no
+// grid-wide barrier (a grid barrier over all SMs costs about 2 us on the
+// GB300, against 5.4 us for an iteration of a CUDA-graph WHILE loop).
+//
+// The chi2 and prior sums reproduce the separate kernels' reductions
+// exactly: the same virtual 256-thread blocks (k_degrid's and
+// k_prior_values' grids), each virtual warp's values on one real warp (the
+// same lanes, so the same shuffle tree), the same tree over the eight warp
+// sums of a virtual block, the same partial slots, and the last block's
+// finishing sums replayed by 256 threads of CTA 0; with the same per-pixel
+// and per-visibility arithmetic (stage_value, the FFT passes, phase_rotated,
+// vis_residual, prior_pixel) every evaluation, and so the search, is
+// bit-identical to the graph loop of separate launches.
 
-struct LinminArgs {
-  FusedArgs<XtImage> f;
-  int prior_a;       // prior-value tasks run in phase A (the rest in phase B)
+constexpr int kClThreads = 512;
+
+struct ClusterLsArgs {
+  StageParams sp;
+  const float* chfreq;
+  float* img;          // the search's point, written back clipped (as the staging kernel does)
+  const uint8_t* mask;
+  const float2* tw;    // FFT twiddles e^{2 pi i m / n}
+  const float* rot_u;
+  const float* rot_v;
+  DegridArgs da;       // channel 0
+  int nb_deg;          // k_degrid's blocks
+  PriorSet<XtImage> ps;
+  int nb_prior;        // k_prior_values' blocks per term
+  int max_pairs;       // virtual-block pairs a CTA takes at most (sizes red)
   LsState* ls;
   double* scal;
-  uint32_t* stop;    // set to 1 by the stepping block when the search is over
-  uint32_t* bar_count;  // grid_sync counters (zero at the launch)
-  uint32_t* bar_epoch;
+  uint32_t* stop;      // 1 once the search is over
 };
+
+// block_sum of a 256-thread block, run by one half of the CTA (threads
+// 0-255: barrier 1, 256-511: barrier 2); the result is valid in the half's
+// first thread.
+__device__ double half_block_sum(double v, double* red8) {
+  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
+  const int bar = 1 + (threadIdx.x >> 8);
+  v = warp_sum(v);
+  if (lane == 0) red8[w] = v;
+  asm volatile("bar.sync %0, 256;" :: "r"(bar) : "memory");
+  double s = 0.0;
+  if (w == 0) {
+    s = lane < 8 ? red8[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  asm volatile("bar.sync %0, 256;" :: "r"(bar) : "memory");
+  return s;
+}
+
+// The per-virtual-block sums of one phase, once every warp has left its
+// virtual warps' shuffle-tree sums in red[p * 16 + warp] (p: the pair of
+// virtual blocks r + kCtas (2p) and r + kCtas (2p + 1); warps 0-7 the
+// first, 8-15 the second): block_sum's second tree per virtual block,
+// stored to part[b].
+template <int kCtas>
+__device__ void vblock_sums(const double* red, int np, int r, int nb, double* part) {
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int task = warp; task < 2 * np; task += kClThreads / 32) {
+    const int p = task >> 1, h = task & 1;
+    const int b = r + kCtas * (2 * p + h);
+    double s = lane < 8 ? red[p * 16 + h * 8 + lane] : 0.0;
+    s = warp_sum(s);
+    if (lane == 0 && b < nb) part[b] = s;
+  }
+  __syncthreads();
+}
+
+// Phase 1: rows [r R, r R + R) at the search's point x (k_rows_fft's
+// arithmetic), row-transformed in rowbuf; then the prior-value partials of
+// this CTA's virtual blocks.
+template <int kCtas>
+__device__ __noinline__ void cl_rows_priors(const ClusterLsArgs& a, float2* rowbuf, double* red, int r,
+                               float x) {
+  const StageParams& sp = a.sp;
+  const int n = sp.N, R = n / kCtas, st = fft_stride(n);
+  const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
+                    sp.flag_opt};
+  const float freq = a.chfreq[0];
+  const float nudiv = freq / sp.nu_0;
+  const float floor_inu = -1.0f * sp.eta * sp.minpix;
+  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
+    const int li = idx >> sp.log2n, j = idx & (n - 1);
+    const int i = r * R + li;
+    const int64_t q = (int64_t)n * i + j;
+    float i0, al;
+    xt_pixel(sp.xs, x, sp.MN, q, i0, al);
+    clip_pixel(a.mask[q], cr, i0, al);
+    if (sp.write_clip) {
+      a.img[q] = i0;
+      a.img[sp.MN + q] = al;
+    }
+    const float arc = beam_arc(__ldg(sp.beam_x + j), __ldg(sp.beam_y + i));
+    rowbuf[li * st + fpad(j)] =
+        make_float2(stage_value(sp, i0, al, arc, freq, nudiv, floor_inu, q), 0.0f);
+  }
+  __syncthreads();
+  smem_fft<kVptLarge>(rowbuf, sp.log2n, R, a.tw);
+  // prior values: virtual block b's thread t sums pixels b 256 + t + j nb 256
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = (warp & 7) * 32 + lane;
+  const int nb = a.nb_prior;
+  const int np = r < nb ? (nb - r + 2 * kCtas - 1) / (2 * kCtas) : 0;
+  for (int u = 0; u < a.ps.n; u++) {
+    const PriorParams& pp = a.ps.pp[u];
+    XtImage I = a.ps.img[u];
+    I.bind();
+    for (int p = 0; p < np; p++) {
+      const int b = r + kCtas * (2 * p + (warp >> 3));
+      CompSum acc;
+      if (b < nb) {
+        for (int64_t q = (int64_t)b * 256 + t; q < pp.MN; q += (int64_t)nb * 256) {
+          if (!(a.mask[q] & kMaskIn)) continue;
+          const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
+          acc.add(prior_pixel(pp, I, i, j));
+        }
+      }
+      const double v = warp_sum(acc.value());
+      if (lane == 0) red[p * 16 + warp] = v;
+    }
+    vblock_sums<kCtas>(red, np, r, nb, a.ps.part[u]);
+  }
+}
+
+// Phase 2: columns [r R, r R + R), gathered from the CTAs' row transforms,
+// column-transformed and phase-rotated in colbuf.
+template <int kCtas>
+__device__ __noinline__ void cl_cols(const ClusterLsArgs& a, float2* const* rows_of, float2* colbuf, int r) {
+  const int n = a.sp.N, R = n / kCtas, st = fft_stride(n);
+  const int lR = __ffs(R) - 1;
+  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
+    const int cc = idx & (R - 1), row = idx >> lR;
+    colbuf[cc * st + fpad(row)] = rows_of[row >> lR][(row & (R - 1)) * st + fpad(r * R + cc)];
+  }
+  __syncthreads();
+  smem_fft<kVptLarge>(colbuf, a.sp.log2n, R, a.tw);
+  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
+    const int cc = idx & (R - 1), row = idx >> lR;
+    float2& g = colbuf[cc * st + fpad(row)];
+    g = phase_rotated(g, __ldg(a.rot_u + r * R + cc), __ldg(a.rot_v + row));
+  }
+}
+
+// Phase 3: the chi2 partials of this CTA's virtual blocks of k_degrid
+// (virtual thread t of block b: visibilities b 256 + t + j nb 256), the
+// grid cells read from the CTAs holding their columns.
+template <int kCtas>
+__device__ __noinline__ void cl_degrid(const ClusterLsArgs& a, float2* const* cols_of, double* red, int r) {
+  const DegridArgs& da = a.da;
+  const ChanRange rg = da.ranges[0];
+  const int n = da.N, R = n / kCtas, st = fft_stride(n), nm1 = n - 1;
+  const int lR = __ffs(R) - 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = (warp & 7) * 32 + lane;
+  const int nb = a.nb_deg;
+  const int np = r < nb ? (nb - r + 2 * kCtas - 1) / (2 * kCtas) : 0;
+  auto cell = [&](int row, int col) -> float2 {
+    return cols_of[col >> lR][(col & (R - 1)) * st + fpad(row)];
+  };
+  if ((int64_t)nb * 256 >= rg.ngrid) {
+    // at most one visibility per virtual thread: four pairs' loads in flight
+    constexpr int kU = 4;
+    for (int p0 = 0; p0 < np; p0 += kU) {
+      float4 d[kU];
+      float2 o[kU], v11[kU], v12[kU], v21[kU], v22[kU];
+      bool has[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int b = r + kCtas * (2 * (p0 + u) + (warp >> 3));
+        const int64_t k = (int64_t)b * 256 + t;
+        has[u] = p0 + u < np && b < nb && k < rg.ngrid;
+        if (has[u]) {
+          d[u] = __ldg(da.deg + rg.off + k);
+          o[u] = __ldg(da.vo + rg.off + k);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        if (has[u]) {
+          const uint32_t c = __float_as_uint(d[u].x);
+          const int i1 = c & 0xffff, j1 = c >> 16;
+          const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
+          v11[u] = cell(j1, i1);
+          v12[u] = cell(j2, i1);
+          v21[u] = cell(j1, i2);
+          v22[u] = cell(j2, i2);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        CompSum acc;
+        if (has[u]) {
+          float rr, ri;
+          vis_residual(d[u], o[u], v11[u], v12[u], v21[u], v22[u], rr, ri);
+          acc.add(chi2_term(d[u].w, rr, ri));
+        }
+        const double v = warp_sum(acc.value());
+        if (lane == 0 && p0 + u < np) red[(p0 + u) * 16 + warp] = v;
+      }
+    }
+  } else {
+    for (int p = 0; p < np; p++) {
+      const int b = r + kCtas * (2 * p + (warp >> 3));
+      CompSum acc;
+      if (b < nb) {
+        for (int64_t k = (int64_t)b * 256 + t; k < rg.ngrid; k += (int64_t)nb * 256) {
+          const float4 d = __ldg(da.deg + rg.off + k);
+          const float2 o = __ldg(da.vo + rg.off + k);
+          const uint32_t c = __float_as_uint(d.x);
+          const int i1 = c & 0xffff, j1 = c >> 16;
+          const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
+          float rr, ri;
+          vis_residual(d, o, cell(j1, i1), cell(j2, i1), cell(j1, i2), cell(j2, i2), rr, ri);
+          acc.add(chi2_term(d.w, rr, ri));
+        }
+      }
+      const double v = warp_sum(acc.value());
+      if (lane == 0) red[p * 16 + warp] = v;
+    }
+  }
+  vblock_sums<kCtas>(red, np, r, nb, da.part);
+}
 
 // the search's step, out of line: one thread once per evaluation, so its
 // state copy and branches do not weigh on the kernel's registers
@@ -910,63 +1117,67 @@ __device__ __noinline__ uint32_t linmin_step(LsState* ls, double* scal) {
   return ls::ls_step(ls, scal) ? 0u : 1u;
 }
 
-// The phases of one evaluation, out of line so that each is register-
-// allocated on its own.
-__device__ __noinline__ void linmin_phase_a(const LinminArgs& a, float2* sm) {
-  const FusedArgs<XtImage>& f = a.f;
-  const int n = f.sp.N, nrow = n * f.C;
-  for (int t = blockIdx.x; t < nrow + a.prior_a; t += gridDim.x) {
-    if (t < nrow) {
-      row_task<kVptSmall>(f.sp, f.chfreq, f.img, f.mask, f.tw, const_cast<float2*>(f.da.grid), sm,
-                          t % n, t / n);
-    } else {
-      const int u = t - nrow;
-      prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
+// Phase 4 (CTA 0): the last blocks' finishing sums -- chi2 (finish_chi2 for
+// one channel, threads 0-255) and the prior values (threads 256-511) --
+// then the search's step by thread 0.
+__device__ __noinline__ void cl_finish_step(const ClusterLsArgs& a, double* red16) {
+  const DegridArgs& da = a.da;
+  const int tl = threadIdx.x & 255;
+  if (threadIdx.x < 256) {
+    double v = 0.0;
+    for (int b = tl; b < a.nb_deg; b += 256) v += __ldcg(da.part + b);
+    v = half_block_sum(v, red16);
+    if (tl == 0) {
+      if (da.normalize && da.nvis[0] > 0) v /= (double)da.nvis[0];
+      double tot = 0.0;
+      tot += v;
+      *da.chi2_out = 0.5 * tot;
+      if (da.term_out) *da.term_out = *da.chi2_out;
+      for (int t = 0; t < 32; t++)
+        if (da.zero_terms & (1u << t)) da.term_slots[t] = 0.0;
     }
-    __syncthreads();
-  }
-}
-
-__device__ __noinline__ void linmin_phase_b(const LinminArgs& a, float2* sm) {
-  const FusedArgs<XtImage>& f = a.f;
-  const int n = f.sp.N, ncg = n / f.cb, ncol = ncg * f.C;
-  const int nprior = f.nb_prior * f.ps.n;
-  for (int t = blockIdx.x; t < ncol + nprior - a.prior_a; t += gridDim.x) {
-    if (t < ncol) {
-      col_task<true, kVptSmall>(n, f.sp.log2n, f.cb, f.rot_u, f.rot_v, f.tw,
-                                const_cast<float2*>(f.da.grid) + (int64_t)(t / ncg) * f.sp.MN, sm,
-                                (t % ncg) * f.cb);
-    } else {
-      const int u = a.prior_a + t - ncol;
-      prior_task(f.ps, f.mask, f.prior_done, u % f.nb_prior, f.nb_prior, u / f.nb_prior);
-    }
-    __syncthreads();
-  }
-}
-
-__device__ __noinline__ void linmin_phase_c(const LinminArgs& a) {
-  const FusedArgs<XtImage>& f = a.f;
-  for (int t = blockIdx.x; t < f.nb_deg * f.C; t += gridDim.x) {
-    if (degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C) && threadIdx.x == 0) {
-      *a.stop = linmin_step(a.ls, a.scal);
-      __threadfence();
+  } else {
+    for (int u = 0; u < a.ps.n; u++) {
+      double v = 0.0;
+      for (int k = tl; k < a.nb_prior; k += 256) v += __ldcg(a.ps.part[u] + k);
+      v = half_block_sum(v, red16 + 8);
+      if (tl == 0) *a.ps.out[u] = v;
     }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) *a.stop = linmin_step(a.ls, a.scal);
 }
 
-// kBps: the blocks per SM the registers are budgeted for (2: 128 a thread,
-// 3: 80, with the degridding phase spilling a little)
-template <int kBps>
-__global__ void __launch_bounds__(256, kBps) k_linmin_fused(const __grid_constant__ LinminArgs a) {
-  extern __shared__ float2 sm[];
-  for (uint32_t k = 0;; k += 3) {
-    linmin_phase_a(a, sm);  // rows at the search's point, prior values
-    if (!grid_sync(a.bar_count, a.bar_epoch, k, a.f.err)) return;
-    linmin_phase_b(a, sm);  // columns, the remaining prior values
-    if (!grid_sync(a.bar_count, a.bar_epoch, k + 1, a.f.err)) return;
-    linmin_phase_c(a);      // degridding and chi2, then the search's step
-    if (!grid_sync(a.bar_count, a.bar_epoch, k + 2, a.f.err)) return;
-    if (__ldcg(a.stop) != 0u) return;
+template <int kCtas>
+__global__ void __launch_bounds__(kClThreads, 1)
+    k_linmin_cluster(const __grid_constant__ ClusterLsArgs a) {
+  extern __shared__ __align__(16) unsigned char cl_smem[];
+  __shared__ float2* rows_of[kCtas];
+  __shared__ float2* cols_of[kCtas];
+  __shared__ double red16[16];
+  cg::cluster_group cl = cg::this_cluster();
+  const int r = (int)cl.block_rank();
+  const int n = a.sp.N, R = n / kCtas, st = fft_stride(n);
+  float2* rowbuf = reinterpret_cast<float2*>(cl_smem);
+  float2* colbuf = rowbuf + R * st;
+  double* red = reinterpret_cast<double*>(colbuf + R * st);
+  if (threadIdx.x < kCtas) {
+    rows_of[threadIdx.x] = cl.map_shared_rank(rowbuf, (unsigned)threadIdx.x);
+    cols_of[threadIdx.x] = cl.map_shared_rank(colbuf, (unsigned)threadIdx.x);
+  }
+  __syncthreads();
+  // every CTA runs the same phases and barriers until the search is over
+  // (the step ends it at its evaluation cap at the latest)
+  for (;;) {
+    cl_rows_priors<kCtas>(a, rowbuf, red, r, __ldcg(a.sp.xs.x_dev));
+    cl.sync();
+    cl_cols<kCtas>(a, rows_of, colbuf, r);
+    cl.sync();
+    cl_degrid<kCtas>(a, cols_of, red, r);
+    cl.sync();
+    if (r == 0) cl_finish_step(a, red16);
+    cl.sync();
+    if (__ldcg(a.stop) != 0u) break;
   }
 }
 
@@ -1476,11 +1687,71 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
   return GV_OK;
 }
 
-// Images up to 512 x 512 with k_degrid's default block size (the fused tasks
-// reproduce its 256-thread blocks), no caller running several problems at
-// once, and GV_LS_FUSED not 0 at creation.
-bool linmin_fused_ok(const Problem& P) {
-  return P.ls_fused && P.fused_off == 0 && P.N <= 512 && P.degrid_threads == 256;
+// k_linmin_cluster<kCtas>: its configuration, and whether this GPU can run
+// one cluster of it (16 CTAs is a non-portable cluster size).
+template <int kCtas>
+static size_t cluster_smem(const Problem& P, int max_pairs) {
+  const int R = P.N / kCtas;
+  return 2 * sizeof(float2) * (size_t)R * fft_stride(P.N) + sizeof(double) * 16 * (size_t)max_pairs;
+}
+
+template <int kCtas>
+static cudaLaunchConfig_t cluster_config(const Problem& P, size_t smem, cudaLaunchAttribute* at) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kCtas);
+  cfg.blockDim = dim3(kClThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = P.stream;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+static int max_pairs(const Problem& P, int ctas) {
+  const int nb = std::max(degrid_blocks(P), prior_blocks(P));
+  return std::max(1, (nb + 2 * ctas - 1) / (2 * ctas));
+}
+
+template <int kCtas>
+static bool cluster_fits(const Problem& P) {
+  const size_t smem = cluster_smem<kCtas>(P, max_pairs(P, kCtas));
+  if (smem > 227 * 1024) return false;
+  if (cudaFuncSetAttribute(k_linmin_cluster<kCtas>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess ||
+      (kCtas > 8 && cudaFuncSetAttribute(k_linmin_cluster<kCtas>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                         1) != cudaSuccess)) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchAttribute at[1];
+  const cudaLaunchConfig_t cfg = cluster_config<kCtas>(P, smem, at);
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, k_linmin_cluster<kCtas>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return clusters >= 1;
+}
+
+// Single-channel images of 64 to 256 pixels a side with k_degrid's default
+// block size (the cluster replays its 256-thread blocks), no caller running
+// several problems at once, GV_LS_FUSED not 0 at creation, and a cluster of
+// 16 (else 8) CTAs that fits this GPU (GV_LS_CTAS=8 at creation: 8).
+bool linmin_fused_ok(Problem& P) {
+  if (!P.ls_fused || P.fused_off != 0 || P.chans.size() != 1 || P.N < 64 || P.N > 256 ||
+      P.degrid_threads != 256)
+    return false;
+  if (P.ls_cluster_ctas == 0) {
+    P.ls_cluster_ctas = -1;
+    if (P.ls_cluster_request != 8 && cluster_fits<16>(P)) P.ls_cluster_ctas = 16;
+    else if (cluster_fits<8>(P)) P.ls_cluster_ctas = 8;
+  }
+  return P.ls_cluster_ctas > 0;
 }
 
 gv_status linmin_fused_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
@@ -1499,59 +1770,46 @@ gv_status linmin_fused_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
     set_error("a line-search evaluation needs the Chi2 term");
     return GV_ERR_UNSUPPORTED;
   }
-  PriorSet<XtImage> ps{};
+  if (!linmin_fused_ok(P)) {
+    set_error("the single-launch line search does not take this problem");
+    return GV_ERR_UNSUPPORTED;
+  }
+  ClusterLsArgs a{};
   const int64_t MN = (int64_t)P.M * P.N;
   const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
                     flag_opt};
   for (size_t t = 0; t < P.terms.size(); t++) {
     const Term& tm = P.terms[t];
     if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
-    const int k = ps.n++;
-    ps.pp[k] = prior_params(P, tm);
-    ps.img[k] = XtImage{xs, P.d_mask, MN, cr, tm.image_index, 0.0f};
-    ps.part[k] = prior_part(P, (int)t);
-    ps.out[k] = P.d_scal + kSlotTerm0 + t;
+    const int k = a.ps.n++;
+    a.ps.pp[k] = prior_params(P, tm);
+    a.ps.img[k] = XtImage{xs, P.d_mask, MN, cr, tm.image_index, 0.0f};
+    a.ps.part[k] = prior_part(P, (int)t);
+    a.ps.out[k] = P.d_scal + kSlotTerm0 + t;
   }
-  const int n = P.N, C = (int)P.chans.size();
-  LinminArgs a{};
-  a.f = fused_args(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero, ps);
+  a.sp = stage_params(P, flag_opt, 1, &xs);
+  a.chfreq = P.d_chfreq;
+  a.img = d_xt;
+  a.mask = P.d_mask;
+  a.tw = P.d_twiddle;
+  a.rot_u = P.d_rot_u;
+  a.rot_v = P.d_rot_v;
+  a.da = degrid_args(P, false, P.d_scal + kSlotTerm0 + ichi2, zero);
+  a.nb_deg = degrid_blocks(P);
+  a.nb_prior = prior_blocks(P);
+  a.max_pairs = max_pairs(P, P.ls_cluster_ctas);
   a.ls = ls;
   a.scal = P.d_scal;
   a.stop = P.d_flags + kFlagLsStop;
-  a.bar_count = P.d_flags + kFlagLsBarCount;
-  a.bar_epoch = P.d_flags + kFlagLsBarEpoch;
-  const size_t smem = sizeof(float2) * (size_t)a.f.cb * fft_stride(n);
-  const int bps = P.ls_blocks_per_sm == 3 ? 3 : 2;
-  auto kern = bps == 3 ? k_linmin_fused<3> : k_linmin_fused<2>;
-  if (P.linmin_blocks == 0) {
-    // every block resident at once: the occupancy bound, at most bps blocks
-    // per SM, and no more than the largest phase has tasks
-    int occ = 0;
-    GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
-    if (occ < 1) {
-      set_error("k_linmin_fused does not fit on an SM");
-      return GV_ERR_UNSUPPORTED;
-    }
-    const int tasks = std::max(n * C + a.f.nb_prior * kMaxTerms, a.f.nb_deg * C);
-    P.linmin_blocks = std::max(1, std::min(P.num_sms * std::min(occ, bps), tasks));
-  }
-  const int blocks = P.linmin_blocks;
-  const int nprior = a.f.nb_prior * ps.n;
-  a.prior_a = std::min(nprior, std::max(0, blocks - n * C));
-  GV_CUDA(cudaMemsetAsync(a.bar_count, 0,
-                          sizeof(uint32_t) * (kFlagLsBarEpoch - kFlagLsBarCount + 1), P.stream));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(blocks);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = P.stream;
   cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  GV_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
-  GV_LAUNCH("k_linmin_fused");
+  if (P.ls_cluster_ctas == 16) {
+    const cudaLaunchConfig_t cfg = cluster_config<16>(P, cluster_smem<16>(P, a.max_pairs), at);
+    GV_CUDA(cudaLaunchKernelEx(&cfg, k_linmin_cluster<16>, a));
+  } else {
+    const cudaLaunchConfig_t cfg = cluster_config<8>(P, cluster_smem<8>(P, a.max_pairs), at);
+    GV_CUDA(cudaLaunchKernelEx(&cfg, k_linmin_cluster<8>, a));
+  }
+  GV_LAUNCH("k_linmin_cluster");
   return GV_OK;
 }
 
