@@ -637,8 +637,10 @@ def run_case(name, reps):
     `weighting` (Uniform and Briggs weighting of configuration 1's 35.28M
     visibilities on a 2048^2 grid), `gridding` (the same visibilities
     gridded with the PillBox2D and 7 x 7 PSWF kernels), `objective_cfg1`
-    (two objective evaluations of configuration 1) and
-    `objective_lbfgs_cfg1` (the same, then two L-BFGS iterations)."""
+    (two objective evaluations of configuration 1),
+    `objective_lbfgs_cfg1` (the same, then two L-BFGS iterations) and
+    `objective_2048_4ch` (two objective evaluations of configuration 1
+    reduced to four channels)."""
     import dataclasses
     import torch
     import gpuvmem_gb300 as gv
@@ -678,10 +680,17 @@ def run_case(name, reps):
         print(json.dumps({"case": name, "visibilities": int(off[-1]), "grid": cfg.n,
                           "channels": len(freqs), "kernels": out}))
         return
-    if name in ("objective_cfg1", "objective_lbfgs_cfg1"):
+    if name in ("objective_cfg1", "objective_lbfgs_cfg1", "objective_2048_4ch"):
         # configuration 1 with chi2 + entropy + TSV: two objective evaluations
-        # (priors on), then (second case) two L-BFGS iterations
-        data = synth.generate(synth.CONFIG1, device="cuda")
+        # (priors on), then (second case) two L-BFGS iterations; the third
+        # case is configuration 1 reduced to four channels at natural weights
+        # and 16 s integrations (4.41M visibilities, grids of 134 MB: above
+        # the L2), for single-kernel profiles
+        cfg = synth.CONFIG1
+        if name == "objective_2048_4ch":
+            cfg = dataclasses.replace(cfg, freqs_hz=list(np.linspace(225e9, 235e9, 4)),
+                                      weighting="natural", dt_s=16.0)
+        data = synth.generate(cfg, device="cuda")
         prob = gv.Problem(data, [gv.term("Chi2", 1.0), gv.term("Entropy", 0.01),
                                  gv.term("TotalSquaredVariation", 1e-4)])
         img = prob.initial_image()

@@ -46,7 +46,6 @@ enum FlagSlot {
   kFlagDegridDone = 4,  // blocks of k_degrid done (the last one finishes chi2)
   kFlagPriorDone = 5,   // blocks of k_prior_values done (the last one sums)
   kFlagOptDone = 6,     // blocks of an optimiser reduction done (the last one sums)
-  kFlagLsStop = 7,      // a single-launch line search is over (k_linmin_cluster)
   kFlagBarCount = 8,    // grid barrier of k_objective_fused: arrivals
   kFlagBarGen = 9,      // grid barrier of k_objective_fused: generation
   kNumFlags = 10
@@ -154,10 +153,6 @@ struct Problem {
                                  // (GV_FUSED=1 at creation turns it on)
   int fused_off = 0;             // > 0 while callers that run problems concurrently launch
   int fused_blocks[3] = {0, 0, 0};  // cooperative blocks of k_objective_fused (per image kind)
-  int ls_fused = 1;              // small images: a line search as one cluster launch
-                                 // (GV_LS_FUSED=0 at creation turns it off)
-  int ls_cluster_request = 16;   // CTAs of that cluster: 16, else 8 (GV_LS_CTAS=8: 8)
-  int ls_cluster_ctas = 0;       // chosen on first use (0: not yet, -1: no cluster fits)
   void* graphs = nullptr;        // graph cache (graph.cu)
   void* ls_graphs = nullptr;     // device line-search graphs (optim.cu)
   struct LsState* d_ls = nullptr;  // device line-search state
@@ -350,11 +345,6 @@ gv_status batch_objective_launch(int np, const void* d_args, const int* d_off, i
                                  cudaStream_t st);
 gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
                               cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
-// A whole line search (from the state k_ls_begin left in ls) as one
-// cluster launch, for the problems linmin_fused_ok accepts
-bool linmin_fused_ok(Problem& P);
-gv_status linmin_fused_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
-                              LsState* ls);
 gv_status fetch_scalars(Problem& P, int n);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);

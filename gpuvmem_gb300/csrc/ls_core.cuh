@@ -247,20 +247,13 @@ __device__ inline bool ls_advance(LsState& s, float f) {
   }
 }
 
-// One step of the search after an evaluation: f is ObjectiveFunction's
-// calcFunction from the term values in scal (sum of lambda_t * value_t in
-// FP64, rounded to float); the search advances to its next point (true) or
-// ends (false), also after `cap` evaluations (error 1).  At the end fret, the
-// evaluation count, the error flag and xmin go to scal[kSlotLs..kSlotLs+3].
-// The state and the term values are read through L2, so the thread that
-// steps may run on a different SM from one evaluation to the next.
-__device__ inline bool ls_step(LsState* gs, double* scal) {
-  LsState s;
-  {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(gs);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&s);
-    for (int i = 0; i < (int)(sizeof(LsState) / sizeof(uint32_t)); i++) dst[i] = __ldcg(src + i);
-  }
+// One step of the search after an evaluation, on a state the caller holds:
+// f is ObjectiveFunction's calcFunction from the term values in scal (sum of
+// lambda_t * value_t in FP64, rounded to float); the search advances to its
+// next point (true) or ends (false), also after `cap` evaluations (error 1).
+// At the end fret, the evaluation count, the error flag and xmin go to
+// scal[kSlotLs..kSlotLs+3].  The term values are read through L2.
+__device__ inline bool ls_step_on(LsState& s, double* scal) {
   double fd = 0.0;
   for (int t = 0; t < s.nterms; t++) fd += ls_dmul((double)s.lambda[t], __ldcg(scal + kSlotTerm0 + t));
   s.evals++;
@@ -278,6 +271,19 @@ __device__ inline bool ls_step(LsState* gs, double* scal) {
     scal[kSlotLs + 2] = (double)s.error;
     scal[kSlotLs + 3] = (double)s.xmin;
   }
+  return more;
+}
+
+// The same on the state in global memory, read through L2 (the thread that
+// steps may run on a different SM from one evaluation to the next).
+__device__ inline bool ls_step(LsState* gs, double* scal) {
+  LsState s;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(gs);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&s);
+    for (int i = 0; i < (int)(sizeof(LsState) / sizeof(uint32_t)); i++) dst[i] = __ldcg(src + i);
+  }
+  const bool more = ls_step_on(s, scal);
   *gs = s;
   return more;
 }

@@ -24,8 +24,6 @@
 #include <cstdlib>
 #include <cstring>
 
-#include <cooperative_groups.h>
-
 #include "gv_internal.cuh"
 #include "ls_core.cuh"
 
@@ -33,10 +31,16 @@ namespace gv {
 
 namespace {
 
-namespace cg = cooperative_groups;
 
+// The arithmetic that more than one kernel performs on the same values (the
+// FFT butterflies and twiddles, the phase rotation, the degridding's model
+// and chi2 terms, the prior stencils) spells out every multiply-add with
+// rounding intrinsics: the compiler never contracts those, so a separate
+// kernel, a fused one and the cluster line search round each operation
+// alike wherever the code is inlined.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)),
+                     __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 
 // R-point inverse DFT (exp(+2 pi i r s / R), R = 2^LR <= 8) of v in
@@ -49,8 +53,8 @@ __device__ __forceinline__ float2 rot_turn(float2 d, int s, int m) {
   const float c = 0.70710678118654752440f;
   if (s == 0) return d;
   if (m == 4 || s == 2) return make_float2(-d.y, d.x);                 // * i
-  if (s == 1) return make_float2(c * (d.x - d.y), c * (d.x + d.y));    // * (1 + i)/sqrt 2
-  return make_float2(c * (-d.x - d.y), c * (d.x - d.y));               // * (-1 + i)/sqrt 2
+  if (s == 1) return make_float2(__fmul_rn(c, d.x - d.y), __fmul_rn(c, d.x + d.y));  // * (1 + i)/sqrt 2
+  return make_float2(__fmul_rn(c, -d.x - d.y), __fmul_rn(c, d.x - d.y));           // * (-1 + i)/sqrt 2
 }
 
 template <int LR>
@@ -164,11 +168,16 @@ constexpr int kVptSmall = 2;
 
 // evaluateXt at one pixel (k_eval_xt's arithmetic): xt = pcom + x xicom,
 // plane 0 floored when positivity is on, plane 1 free.
+__device__ __forceinline__ void xt_value(const XtSource& xs, float x, float p0, float d0, float p1,
+                                         float d1, float& i0, float& al) {
+  const float v0 = fmaf(x, d0, p0);
+  i0 = (xs.positivity && !(v0 > xs.floor_cmp)) ? xs.floor_val : v0;
+  al = fmaf(x, d1, p1);
+}
+
 __device__ __forceinline__ void xt_pixel(const XtSource& xs, float x, int64_t MN, int64_t q,
                                          float& i0, float& al) {
-  const float v0 = fmaf(x, xs.xicom[q], xs.pcom[q]);
-  i0 = (xs.positivity && !(v0 > xs.floor_cmp)) ? xs.floor_val : v0;
-  al = fmaf(x, xs.xicom[MN + q], xs.pcom[MN + q]);
+  xt_value(xs, x, xs.pcom[q], xs.xicom[q], xs.pcom[MN + q], xs.xicom[MN + q], i0, al);
 }
 
 // What clip2IWNoise (src/functions.cu:2694-2719) leaves at one pixel.
@@ -475,17 +484,19 @@ struct DegridArgs {
 __device__ __forceinline__ void vis_residual(const float4& d, float2 o, float2 v11, float2 v12,
                                              float2 v21, float2 v22, float& rr, float& ri) {
   const float du = d.y, dv = d.z;
-  const float w11 = (1.0f - du) * (1.0f - dv), w12 = (1.0f - du) * dv;
-  const float w21 = du * (1.0f - dv), w22 = du * dv;
-  const float mr = w11 * v11.x + w12 * v12.x + w21 * v21.x + w22 * v22.x;
-  const float mi = w11 * v11.y + w12 * v12.y + w21 * v21.y + w22 * v22.y;
+  const float w11 = __fmul_rn(1.0f - du, 1.0f - dv), w12 = __fmul_rn(1.0f - du, dv);
+  const float w21 = __fmul_rn(du, 1.0f - dv), w22 = __fmul_rn(du, dv);
+  const float mr =
+      __fmaf_rn(w22, v22.x, __fmaf_rn(w21, v21.x, __fmaf_rn(w12, v12.x, __fmul_rn(w11, v11.x))));
+  const float mi =
+      __fmaf_rn(w22, v22.y, __fmaf_rn(w21, v21.y, __fmaf_rn(w12, v12.y, __fmul_rn(w11, v11.y))));
   rr = o.x - mr;
   ri = o.y - mi;
 }
 
 // chi2Vector (src/functions.cu:2867): w |Vr|^2
 __device__ __forceinline__ float chi2_term(float w, float rr, float ri) {
-  return w * (rr * rr + ri * ri);
+  return __fmul_rn(w, __fmaf_rn(rr, rr, __fmul_rn(ri, ri)));
 }
 
 // Pass 3 for block b of nb of channel c: vis_mod + residual + chi2Vector
@@ -568,26 +579,27 @@ __device__ __forceinline__ float prior_pixel(const PriorParams& pp, const Img& I
     case GV_FI_ENTROPY:
       return c * logf((c / pp.G) + (pp.eta + 1.0f));
     case GV_FI_L1:
-      return sqrtf(c * c + pp.eps);
+      return sqrtf(__fmaf_rn(c, c, pp.eps));
     case GV_FI_TSV:
       if (i < N - 1 && j < N - 1) {
         const float dx = c - I[(int64_t)N * i + j + 1];
         const float dy = c - I[(int64_t)N * (i + 1) + j];
-        return dx * dx + dy * dy;
+        return __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
       }
       return c;
     case GV_FI_TV:
       if (i < N - 1 && j < N - 1) {
         const float r = I[(int64_t)N * i + j + 1];
         const float d = I[(int64_t)N * (i + 1) + j];
-        return sqrtf((r - c) * (r - c) + (d - c) * (d - c) + pp.eps);
+        return sqrtf(__fmaf_rn(r - c, r - c, __fmul_rn(d - c, d - c)) + pp.eps);
       }
       return c;
     case GV_FI_LAPLACIAN:
       if (i > 0 && i < N - 1 && j > 0 && j < N - 1) {
-        const float Dx = I[(int64_t)N * i + j - 1] - 2.0f * c + I[(int64_t)N * i + j + 1];
-        const float Dy = I[(int64_t)N * (i - 1) + j] - 2.0f * c + I[(int64_t)N * (i + 1) + j];
-        return 0.5f * (Dx + Dy) * (Dx + Dy);
+        const float c2 = __fmul_rn(2.0f, c);
+        const float Dx = (I[(int64_t)N * i + j - 1] - c2) + I[(int64_t)N * i + j + 1];
+        const float Dy = (I[(int64_t)N * (i - 1) + j] - c2) + I[(int64_t)N * (i + 1) + j];
+        return __fmul_rn(__fmul_rn(0.5f, Dx + Dy), Dx + Dy);
       }
       return c;
     case GV_FI_GENTROPY: {
@@ -596,13 +608,15 @@ __device__ __forceinline__ float prior_pixel(const PriorParams& pp, const Img& I
     }
     case GV_FI_GL1: {
       const float g = pp.prior[(int64_t)N * i + j];
-      return sqrtf(c * c + pp.eps) / (sqrtf(g * g + pp.eps) + pp.eps_b);
+      return sqrtf(__fmaf_rn(c, c, pp.eps)) / (sqrtf(__fmaf_rn(g, g, pp.eps)) + pp.eps_b);
     }
     case GV_FI_QUADRATIC:
       if (i > 0 && i < N - 1 && j > 0 && j < N - 1) {
         const float l = I[(int64_t)N * i + j - 1], r = I[(int64_t)N * i + j + 1];
         const float d = I[(int64_t)N * (i + 1) + j], u = I[(int64_t)N * (i - 1) + j];
-        float qp = (c - l) * (c - l) + (c - r) * (c - r) + (c - u) * (c - u) + (c - d) * (c - d);
+        const float qp = __fmaf_rn(c - d, c - d,
+                                   __fmaf_rn(c - u, c - u,
+                                             __fmaf_rn(c - r, c - r, __fmul_rn(c - l, c - l))));
         return qp / 2.0f;
       }
       return c;
@@ -873,312 +887,6 @@ __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
   // C: degridding and chi2
   for (int t = blockIdx.x; t < f.nb_deg * f.C; t += gridDim.x)
     degrid_task<true>(f.da, t % f.nb_deg, f.nb_deg, t / f.nb_deg, f.C);
-}
-
-// ---- small single-channel images: a whole line search in one cluster -----
-//
-// linmin's search (src/linmin.cu:52-110, the state machine of ls_core.cuh)
-// with every objective evaluation done by one thread-block cluster that
-// keeps the channel's grid on chip.  CTA r of the kCtas stages and
-// row-transforms image rows [r R, r R + R) (R = N / kCtas) into its shared
-// memory; gathers columns [r R, r R + R) of the row transforms from every
-// CTA's shared memory (distributed shared memory), column-transforms and
-// phase-rotates them in place; and the degridding reads each visibility's
-// four cells from the CTAs that hold their columns.  Cluster barriers (in
-// hardware) separate the phases, so the search is one launch with no
-// grid-wide barrier (a grid barrier over all SMs costs about 2 us on the
-// GB300, against 5.4 us for an iteration of a CUDA-graph WHILE loop).
-//
-// The chi2 and prior sums reproduce the separate kernels' reductions
-// exactly: the same virtual 256-thread blocks (k_degrid's and
-// k_prior_values' grids), each virtual warp's values on one real warp (the
-// same lanes, so the same shuffle tree), the same tree over the eight warp
-// sums of a virtual block, the same partial slots, and the last block's
-// finishing sums replayed by 256 threads of CTA 0; with the same per-pixel
-// and per-visibility arithmetic (stage_value, the FFT passes, phase_rotated,
-// vis_residual, prior_pixel) every evaluation, and so the search, is
-// bit-identical to the graph loop of separate launches.
-
-constexpr int kClThreads = 512;
-
-struct ClusterLsArgs {
-  StageParams sp;
-  const float* chfreq;
-  float* img;          // the search's point, written back clipped (as the staging kernel does)
-  const uint8_t* mask;
-  const float2* tw;    // FFT twiddles e^{2 pi i m / n}
-  const float* rot_u;
-  const float* rot_v;
-  DegridArgs da;       // channel 0
-  int nb_deg;          // k_degrid's blocks
-  PriorSet<XtImage> ps;
-  int nb_prior;        // k_prior_values' blocks per term
-  int max_pairs;       // virtual-block pairs a CTA takes at most (sizes red)
-  LsState* ls;
-  double* scal;
-  uint32_t* stop;      // 1 once the search is over
-};
-
-// block_sum of a 256-thread block, run by one half of the CTA (threads
-// 0-255: barrier 1, 256-511: barrier 2); the result is valid in the half's
-// first thread.
-__device__ double half_block_sum(double v, double* red8) {
-  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
-  const int bar = 1 + (threadIdx.x >> 8);
-  v = warp_sum(v);
-  if (lane == 0) red8[w] = v;
-  asm volatile("bar.sync %0, 256;" :: "r"(bar) : "memory");
-  double s = 0.0;
-  if (w == 0) {
-    s = lane < 8 ? red8[lane] : 0.0;
-    s = warp_sum(s);
-  }
-  asm volatile("bar.sync %0, 256;" :: "r"(bar) : "memory");
-  return s;
-}
-
-// The per-virtual-block sums of one phase, once every warp has left its
-// virtual warps' shuffle-tree sums in red[p * 16 + warp] (p: the pair of
-// virtual blocks r + kCtas (2p) and r + kCtas (2p + 1); warps 0-7 the
-// first, 8-15 the second): block_sum's second tree per virtual block,
-// stored to part[b].
-template <int kCtas>
-__device__ void vblock_sums(const double* red, int np, int r, int nb, double* part) {
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int task = warp; task < 2 * np; task += kClThreads / 32) {
-    const int p = task >> 1, h = task & 1;
-    const int b = r + kCtas * (2 * p + h);
-    double s = lane < 8 ? red[p * 16 + h * 8 + lane] : 0.0;
-    s = warp_sum(s);
-    if (lane == 0 && b < nb) part[b] = s;
-  }
-  __syncthreads();
-}
-
-// Phase 1: rows [r R, r R + R) at the search's point x (k_rows_fft's
-// arithmetic), row-transformed in rowbuf; then the prior-value partials of
-// this CTA's virtual blocks.
-template <int kCtas>
-__device__ __noinline__ void cl_rows_priors(const ClusterLsArgs& a, float2* rowbuf, double* red, int r,
-                               float x) {
-  const StageParams& sp = a.sp;
-  const int n = sp.N, R = n / kCtas, st = fft_stride(n);
-  const ClipRule cr{sp.eta > 0.0f ? 0.0f : (float)(-1.0 * sp.eta * sp.minpix), sp.threshold,
-                    sp.flag_opt};
-  const float freq = a.chfreq[0];
-  const float nudiv = freq / sp.nu_0;
-  const float floor_inu = -1.0f * sp.eta * sp.minpix;
-  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
-    const int li = idx >> sp.log2n, j = idx & (n - 1);
-    const int i = r * R + li;
-    const int64_t q = (int64_t)n * i + j;
-    float i0, al;
-    xt_pixel(sp.xs, x, sp.MN, q, i0, al);
-    clip_pixel(a.mask[q], cr, i0, al);
-    if (sp.write_clip) {
-      a.img[q] = i0;
-      a.img[sp.MN + q] = al;
-    }
-    const float arc = beam_arc(__ldg(sp.beam_x + j), __ldg(sp.beam_y + i));
-    rowbuf[li * st + fpad(j)] =
-        make_float2(stage_value(sp, i0, al, arc, freq, nudiv, floor_inu, q), 0.0f);
-  }
-  __syncthreads();
-  smem_fft<kVptLarge>(rowbuf, sp.log2n, R, a.tw);
-  // prior values: virtual block b's thread t sums pixels b 256 + t + j nb 256
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int t = (warp & 7) * 32 + lane;
-  const int nb = a.nb_prior;
-  const int np = r < nb ? (nb - r + 2 * kCtas - 1) / (2 * kCtas) : 0;
-  for (int u = 0; u < a.ps.n; u++) {
-    const PriorParams& pp = a.ps.pp[u];
-    XtImage I = a.ps.img[u];
-    I.bind();
-    for (int p = 0; p < np; p++) {
-      const int b = r + kCtas * (2 * p + (warp >> 3));
-      CompSum acc;
-      if (b < nb) {
-        for (int64_t q = (int64_t)b * 256 + t; q < pp.MN; q += (int64_t)nb * 256) {
-          if (!(a.mask[q] & kMaskIn)) continue;
-          const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
-          acc.add(prior_pixel(pp, I, i, j));
-        }
-      }
-      const double v = warp_sum(acc.value());
-      if (lane == 0) red[p * 16 + warp] = v;
-    }
-    vblock_sums<kCtas>(red, np, r, nb, a.ps.part[u]);
-  }
-}
-
-// Phase 2: columns [r R, r R + R), gathered from the CTAs' row transforms,
-// column-transformed and phase-rotated in colbuf.
-template <int kCtas>
-__device__ __noinline__ void cl_cols(const ClusterLsArgs& a, float2* const* rows_of, float2* colbuf, int r) {
-  const int n = a.sp.N, R = n / kCtas, st = fft_stride(n);
-  const int lR = __ffs(R) - 1;
-  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
-    const int cc = idx & (R - 1), row = idx >> lR;
-    colbuf[cc * st + fpad(row)] = rows_of[row >> lR][(row & (R - 1)) * st + fpad(r * R + cc)];
-  }
-  __syncthreads();
-  smem_fft<kVptLarge>(colbuf, a.sp.log2n, R, a.tw);
-  for (int idx = threadIdx.x; idx < R * n; idx += kClThreads) {
-    const int cc = idx & (R - 1), row = idx >> lR;
-    float2& g = colbuf[cc * st + fpad(row)];
-    g = phase_rotated(g, __ldg(a.rot_u + r * R + cc), __ldg(a.rot_v + row));
-  }
-}
-
-// Phase 3: the chi2 partials of this CTA's virtual blocks of k_degrid
-// (virtual thread t of block b: visibilities b 256 + t + j nb 256), the
-// grid cells read from the CTAs holding their columns.
-template <int kCtas>
-__device__ __noinline__ void cl_degrid(const ClusterLsArgs& a, float2* const* cols_of, double* red, int r) {
-  const DegridArgs& da = a.da;
-  const ChanRange rg = da.ranges[0];
-  const int n = da.N, R = n / kCtas, st = fft_stride(n), nm1 = n - 1;
-  const int lR = __ffs(R) - 1;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int t = (warp & 7) * 32 + lane;
-  const int nb = a.nb_deg;
-  const int np = r < nb ? (nb - r + 2 * kCtas - 1) / (2 * kCtas) : 0;
-  auto cell = [&](int row, int col) -> float2 {
-    return cols_of[col >> lR][(col & (R - 1)) * st + fpad(row)];
-  };
-  if ((int64_t)nb * 256 >= rg.ngrid) {
-    // at most one visibility per virtual thread: four pairs' loads in flight
-    constexpr int kU = 4;
-    for (int p0 = 0; p0 < np; p0 += kU) {
-      float4 d[kU];
-      float2 o[kU], v11[kU], v12[kU], v21[kU], v22[kU];
-      bool has[kU];
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        const int b = r + kCtas * (2 * (p0 + u) + (warp >> 3));
-        const int64_t k = (int64_t)b * 256 + t;
-        has[u] = p0 + u < np && b < nb && k < rg.ngrid;
-        if (has[u]) {
-          d[u] = __ldg(da.deg + rg.off + k);
-          o[u] = __ldg(da.vo + rg.off + k);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        if (has[u]) {
-          const uint32_t c = __float_as_uint(d[u].x);
-          const int i1 = c & 0xffff, j1 = c >> 16;
-          const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
-          v11[u] = cell(j1, i1);
-          v12[u] = cell(j2, i1);
-          v21[u] = cell(j1, i2);
-          v22[u] = cell(j2, i2);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        CompSum acc;
-        if (has[u]) {
-          float rr, ri;
-          vis_residual(d[u], o[u], v11[u], v12[u], v21[u], v22[u], rr, ri);
-          acc.add(chi2_term(d[u].w, rr, ri));
-        }
-        const double v = warp_sum(acc.value());
-        if (lane == 0 && p0 + u < np) red[(p0 + u) * 16 + warp] = v;
-      }
-    }
-  } else {
-    for (int p = 0; p < np; p++) {
-      const int b = r + kCtas * (2 * p + (warp >> 3));
-      CompSum acc;
-      if (b < nb) {
-        for (int64_t k = (int64_t)b * 256 + t; k < rg.ngrid; k += (int64_t)nb * 256) {
-          const float4 d = __ldg(da.deg + rg.off + k);
-          const float2 o = __ldg(da.vo + rg.off + k);
-          const uint32_t c = __float_as_uint(d.x);
-          const int i1 = c & 0xffff, j1 = c >> 16;
-          const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
-          float rr, ri;
-          vis_residual(d, o, cell(j1, i1), cell(j2, i1), cell(j1, i2), cell(j2, i2), rr, ri);
-          acc.add(chi2_term(d.w, rr, ri));
-        }
-      }
-      const double v = warp_sum(acc.value());
-      if (lane == 0) red[p * 16 + warp] = v;
-    }
-  }
-  vblock_sums<kCtas>(red, np, r, nb, da.part);
-}
-
-// the search's step, out of line: one thread once per evaluation, so its
-// state copy and branches do not weigh on the kernel's registers
-__device__ __noinline__ uint32_t linmin_step(LsState* ls, double* scal) {
-  return ls::ls_step(ls, scal) ? 0u : 1u;
-}
-
-// Phase 4 (CTA 0): the last blocks' finishing sums -- chi2 (finish_chi2 for
-// one channel, threads 0-255) and the prior values (threads 256-511) --
-// then the search's step by thread 0.
-__device__ __noinline__ void cl_finish_step(const ClusterLsArgs& a, double* red16) {
-  const DegridArgs& da = a.da;
-  const int tl = threadIdx.x & 255;
-  if (threadIdx.x < 256) {
-    double v = 0.0;
-    for (int b = tl; b < a.nb_deg; b += 256) v += __ldcg(da.part + b);
-    v = half_block_sum(v, red16);
-    if (tl == 0) {
-      if (da.normalize && da.nvis[0] > 0) v /= (double)da.nvis[0];
-      double tot = 0.0;
-      tot += v;
-      *da.chi2_out = 0.5 * tot;
-      if (da.term_out) *da.term_out = *da.chi2_out;
-      for (int t = 0; t < 32; t++)
-        if (da.zero_terms & (1u << t)) da.term_slots[t] = 0.0;
-    }
-  } else {
-    for (int u = 0; u < a.ps.n; u++) {
-      double v = 0.0;
-      for (int k = tl; k < a.nb_prior; k += 256) v += __ldcg(a.ps.part[u] + k);
-      v = half_block_sum(v, red16 + 8);
-      if (tl == 0) *a.ps.out[u] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) *a.stop = linmin_step(a.ls, a.scal);
-}
-
-template <int kCtas>
-__global__ void __launch_bounds__(kClThreads, 1)
-    k_linmin_cluster(const __grid_constant__ ClusterLsArgs a) {
-  extern __shared__ __align__(16) unsigned char cl_smem[];
-  __shared__ float2* rows_of[kCtas];
-  __shared__ float2* cols_of[kCtas];
-  __shared__ double red16[16];
-  cg::cluster_group cl = cg::this_cluster();
-  const int r = (int)cl.block_rank();
-  const int n = a.sp.N, R = n / kCtas, st = fft_stride(n);
-  float2* rowbuf = reinterpret_cast<float2*>(cl_smem);
-  float2* colbuf = rowbuf + R * st;
-  double* red = reinterpret_cast<double*>(colbuf + R * st);
-  if (threadIdx.x < kCtas) {
-    rows_of[threadIdx.x] = cl.map_shared_rank(rowbuf, (unsigned)threadIdx.x);
-    cols_of[threadIdx.x] = cl.map_shared_rank(colbuf, (unsigned)threadIdx.x);
-  }
-  __syncthreads();
-  // every CTA runs the same phases and barriers until the search is over
-  // (the step ends it at its evaluation cap at the latest)
-  for (;;) {
-    cl_rows_priors<kCtas>(a, rowbuf, red, r, __ldcg(a.sp.xs.x_dev));
-    cl.sync();
-    cl_cols<kCtas>(a, rows_of, colbuf, r);
-    cl.sync();
-    cl_degrid<kCtas>(a, cols_of, red, r);
-    cl.sync();
-    if (r == 0) cl_finish_step(a, red16);
-    cl.sync();
-    if (__ldcg(a.stop) != 0u) break;
-  }
 }
 
 // ---- batches: the objectives of several problems in one cooperative launch
@@ -1684,132 +1392,6 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
   gv_status s = chi2_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero);
   if (s != GV_OK) return s;
   if (ps.n > 0) GV_CUDA(cudaStreamWaitEvent(P.stream, join, 0));
-  return GV_OK;
-}
-
-// k_linmin_cluster<kCtas>: its configuration, and whether this GPU can run
-// one cluster of it (16 CTAs is a non-portable cluster size).
-template <int kCtas>
-static size_t cluster_smem(const Problem& P, int max_pairs) {
-  const int R = P.N / kCtas;
-  return 2 * sizeof(float2) * (size_t)R * fft_stride(P.N) + sizeof(double) * 16 * (size_t)max_pairs;
-}
-
-template <int kCtas>
-static cudaLaunchConfig_t cluster_config(const Problem& P, size_t smem, cudaLaunchAttribute* at) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kCtas);
-  cfg.blockDim = dim3(kClThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = P.stream;
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kCtas;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cfg;
-}
-
-static int max_pairs(const Problem& P, int ctas) {
-  const int nb = std::max(degrid_blocks(P), prior_blocks(P));
-  return std::max(1, (nb + 2 * ctas - 1) / (2 * ctas));
-}
-
-template <int kCtas>
-static bool cluster_fits(const Problem& P) {
-  const size_t smem = cluster_smem<kCtas>(P, max_pairs(P, kCtas));
-  if (smem > 227 * 1024) return false;
-  if (cudaFuncSetAttribute(k_linmin_cluster<kCtas>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess ||
-      (kCtas > 8 && cudaFuncSetAttribute(k_linmin_cluster<kCtas>,
-                                         cudaFuncAttributeNonPortableClusterSizeAllowed,
-                                         1) != cudaSuccess)) {
-    cudaGetLastError();
-    return false;
-  }
-  cudaLaunchAttribute at[1];
-  const cudaLaunchConfig_t cfg = cluster_config<kCtas>(P, smem, at);
-  int clusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&clusters, k_linmin_cluster<kCtas>, &cfg) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return clusters >= 1;
-}
-
-// Single-channel images of 64 to 256 pixels a side with k_degrid's default
-// block size (the cluster replays its 256-thread blocks), no caller running
-// several problems at once, GV_LS_FUSED not 0 at creation, and a cluster of
-// 16 (else 8) CTAs that fits this GPU (GV_LS_CTAS=8 at creation: 8).
-bool linmin_fused_ok(Problem& P) {
-  if (!P.ls_fused || P.fused_off != 0 || P.chans.size() != 1 || P.N < 64 || P.N > 256 ||
-      P.degrid_threads != 256)
-    return false;
-  if (P.ls_cluster_ctas == 0) {
-    P.ls_cluster_ctas = -1;
-    if (P.ls_cluster_request != 8 && cluster_fits<16>(P)) P.ls_cluster_ctas = 16;
-    else if (cluster_fits<8>(P)) P.ls_cluster_ctas = 8;
-  }
-  return P.ls_cluster_ctas > 0;
-}
-
-gv_status linmin_fused_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
-                              LsState* ls) {
-  // the terms as ls_objective_launch arranges them
-  int ichi2 = -1;
-  uint32_t zero = 0u;
-  for (size_t t = 0; t < P.terms.size(); t++) {
-    if (P.terms[t].kind == GV_FI_CHI2) {
-      if (ichi2 < 0) ichi2 = (int)t;
-    } else if (!(P.iteration > 0 && P.terms[t].lambda != 0.0f)) {
-      zero |= 1u << t;
-    }
-  }
-  if (ichi2 < 0) {
-    set_error("a line-search evaluation needs the Chi2 term");
-    return GV_ERR_UNSUPPORTED;
-  }
-  if (!linmin_fused_ok(P)) {
-    set_error("the single-launch line search does not take this problem");
-    return GV_ERR_UNSUPPORTED;
-  }
-  ClusterLsArgs a{};
-  const int64_t MN = (int64_t)P.M * P.N;
-  const ClipRule cr{P.eta > 0.0f ? 0.0f : (float)(-1.0 * P.eta * P.minpix), P.threshold,
-                    flag_opt};
-  for (size_t t = 0; t < P.terms.size(); t++) {
-    const Term& tm = P.terms[t];
-    if (tm.kind == GV_FI_CHI2 || (zero & (1u << t))) continue;
-    const int k = a.ps.n++;
-    a.ps.pp[k] = prior_params(P, tm);
-    a.ps.img[k] = XtImage{xs, P.d_mask, MN, cr, tm.image_index, 0.0f};
-    a.ps.part[k] = prior_part(P, (int)t);
-    a.ps.out[k] = P.d_scal + kSlotTerm0 + t;
-  }
-  a.sp = stage_params(P, flag_opt, 1, &xs);
-  a.chfreq = P.d_chfreq;
-  a.img = d_xt;
-  a.mask = P.d_mask;
-  a.tw = P.d_twiddle;
-  a.rot_u = P.d_rot_u;
-  a.rot_v = P.d_rot_v;
-  a.da = degrid_args(P, false, P.d_scal + kSlotTerm0 + ichi2, zero);
-  a.nb_deg = degrid_blocks(P);
-  a.nb_prior = prior_blocks(P);
-  a.max_pairs = max_pairs(P, P.ls_cluster_ctas);
-  a.ls = ls;
-  a.scal = P.d_scal;
-  a.stop = P.d_flags + kFlagLsStop;
-  cudaLaunchAttribute at[1];
-  if (P.ls_cluster_ctas == 16) {
-    const cudaLaunchConfig_t cfg = cluster_config<16>(P, cluster_smem<16>(P, a.max_pairs), at);
-    GV_CUDA(cudaLaunchKernelEx(&cfg, k_linmin_cluster<16>, a));
-  } else {
-    const cudaLaunchConfig_t cfg = cluster_config<8>(P, cluster_smem<8>(P, a.max_pairs), at);
-    GV_CUDA(cudaLaunchKernelEx(&cfg, k_linmin_cluster<8>, a));
-  }
-  GV_LAUNCH("k_linmin_cluster");
   return GV_OK;
 }
 

@@ -665,37 +665,8 @@ class Solver {
     return GV_OK;
   }
 
-  // linmin on the GPU, small images: the whole search and its evaluations
-  // as one cooperative launch
-  gv_status linmin_fused(float* p, float* xi, float* fret) {
-    LsTerms terms{};
-    terms.nterms = (int)P_.terms.size();
-    for (size_t t = 0; t < P_.terms.size(); t++) terms.lambda[t] = P_.terms[t].lambda;
-    GV_CUDA(cudaMemcpyAsync(w_.pcom, p, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
-    GV_CUDA(cudaMemcpyAsync(w_.xicom, xi, sizeof(float) * 2 * MN_, cudaMemcpyDeviceToDevice, P_.stream));
-    GV_TRY(ls_begin_launch(P_.stream, P_.d_ls, terms, 1.0e-7f, kLsCap));
-    const XtSource xs{w_.pcom, w_.xicom, &P_.d_ls->x_req, floor_val_, floor_cmp_, o_.positivity};
-    GV_TRY(linmin_fused_launch(P_, w_.xt, o_.flag, xs, P_.d_ls));
-    k_new_p<<<nblk(2 * MN_), 256, 0, P_.stream>>>(MN_, 0.0f, &P_.d_ls->xmin, floor_val_,
-                                                   floor_cmp_, o_.positivity, p, xi);
-    GV_LAUNCH("k_new_p");
-    GV_TRY(fetch_scalars(P_, kSlotLs + 4));
-    GV_TRY(check_device_error(P_));
-    n_obj_ += (int64_t)P_.h_scal[kSlotLs + 1];
-    *fret = (float)P_.h_scal[kSlotLs];
-    if (P_.h_scal[kSlotLs + 2] != 0.0) {
-      set_error("line search did not end within its evaluation limit (unbounded along the line?)");
-      return GV_ERR_DEVICE;
-    }
-    if (verbose())
-      std::fprintf(stderr, "Alpha for linear minimization = %.9g (f = %.9g)\n",
-                   (float)P_.h_scal[kSlotLs + 3], *fret);
-    return GV_OK;
-  }
-
   // linmin on the GPU: the whole bracket + Brent search as one graph launch
   gv_status linmin_device(float* p, float* xi, float* fret) {
-    if (linmin_fused_ok(P_)) return linmin_fused(p, xi, fret);
     LsCache& c = ls_cache(P_);
     const int gate = P_.iteration > 0 ? 1 : 0;
     LsEntry* hit = nullptr;

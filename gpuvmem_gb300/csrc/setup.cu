@@ -697,8 +697,6 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
     P.use_graphs = (g && g[0] == '0') ? 0 : 1;
   }
   if (const char* e = std::getenv("GV_FUSED")) P.fused = std::atoi(e) != 0 ? 1 : 0;
-  if (const char* e = std::getenv("GV_LS_FUSED")) P.ls_fused = std::atoi(e) != 0 ? 1 : 0;
-  if (const char* e = std::getenv("GV_LS_CTAS")) P.ls_cluster_request = std::atoi(e) == 8 ? 8 : 16;
   P.part_stride = 4 * P.num_sms;
   const int nslots = C + kMaxTerms + 8;
   GV_CUDA(cudaMalloc(&P.d_part, sizeof(double) * (size_t)P.part_stride * nslots));

@@ -257,9 +257,9 @@ gv_status gv_optimize_until(gv_problem* p, const gv_opt_desc* opt, float* d_img,
  * floored at -eta*MINPIX with positivity (its d_xi then 0).  *fret is the
  * objective at the minimum and *evals (may be null) the evaluations the search
  * took.  d_p and d_xi are device images (2 x M x N floats).  The priors count
- * as Fi::iteration (gv_set_iteration) says.  Images up to 512 x 512 run the
- * whole search as one cooperative launch (GV_LS_FUSED=0 at creation: a CUDA
- * graph loop of separate launches); results are identical either way. */
+ * as Fi::iteration (gv_set_iteration) says.  The search runs on the GPU as
+ * one CUDA-graph launch (a WHILE loop over the evaluations) when graphs are
+ * on, else on the host; the two visit the same points. */
 gv_status gv_linmin(gv_problem* p, float* d_p, float* d_xi, int32_t flag_opt,
                     int32_t positivity, float* fret, int64_t* evals);
 
