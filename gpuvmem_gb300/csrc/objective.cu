@@ -385,10 +385,21 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
                                          float2* __restrict__ G, float2* buf, int j0) {
   const int n = N;
   const int lcb = __ffs(cb) - 1;  // cb is a power of two
-  for (int idx = threadIdx.x; idx < cb * n; idx += blockDim.x) {
-    const int r = idx >> lcb, cc = idx & (cb - 1);
-    const float2* src = G + (int64_t)n * r + j0 + cc;
-    buf[cc * fft_stride(n) + fpad(r)] = kL2Loads ? __ldcg(src) : *src;
+  // every load of the thread first (cb n <= VPT blockDim.x), then the stores:
+  // the loads are in flight together
+  float2 v[VPT];
+#pragma unroll
+  for (int k = 0; k < VPT; k++) {
+    const int idx = threadIdx.x + k * blockDim.x;
+    if (idx < cb * n) {
+      const float2* src = G + (int64_t)n * (idx >> lcb) + j0 + (idx & (cb - 1));
+      v[k] = kL2Loads ? __ldcg(src) : *src;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < VPT; k++) {
+    const int idx = threadIdx.x + k * blockDim.x;
+    if (idx < cb * n) buf[(idx & (cb - 1)) * fft_stride(n) + fpad(idx >> lcb)] = v[k];
   }
   __syncthreads();
   smem_fft<VPT>(buf, log2n, cb, tw);

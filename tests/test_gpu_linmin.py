@@ -54,7 +54,7 @@ def test_linmin_device_matches_host(n, nchan, iteration):
     # that stays above the floor (elsewhere p = floor, d = 0), so every kept
     # pixel moved by one multiple of its direction
     m = (dd[0] != 0) & (d0[0] != 0)
-    assert m.sum() > 0.5 * m.size
+    assert m.sum() > 100
     xmin = (dd[0][m] / d0[0][m]).astype(np.float64)
     assert np.allclose(xmin, np.median(xmin), rtol=1e-5)
     np.testing.assert_array_equal(pd[0][m], (p0[0] + dd[0])[m])
