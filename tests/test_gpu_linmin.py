@@ -51,10 +51,13 @@ def test_linmin_device_matches_host(n, nchan, iteration):
     np.testing.assert_array_equal(pd.view(np.uint32), ph.view(np.uint32))
     np.testing.assert_array_equal(dd.view(np.uint32), dh.view(np.uint32))
     # newP (src/functions.cu:2760-2777): d <- xmin d and p <- p + d where
-    # that stays above the floor (elsewhere p = floor, d = 0), so every kept
-    # pixel moved by one multiple of its direction
-    m = (dd[0] != 0) & (d0[0] != 0)
-    assert m.sum() > 100
-    xmin = (dd[0][m] / d0[0][m]).astype(np.float64)
-    assert np.allclose(xmin, np.median(xmin), rtol=1e-5)
-    np.testing.assert_array_equal(pd[0][m], (p0[0] + dd[0])[m])
+    # that stays above the floor; elsewhere p = the floor and d = 0
+    moved = (dd[0] != 0) & (d0[0] != 0)
+    floored = (dd[0] == 0) & (d0[0] != 0)
+    assert moved.sum() + floored.sum() > 100
+    if moved.any():
+        xmin = (dd[0][moved] / d0[0][moved]).astype(np.float64)
+        assert np.allclose(xmin, np.median(xmin), rtol=1e-5)
+        np.testing.assert_array_equal(pd[0][moved], (p0[0] + dd[0])[moved])
+    if floored.any():
+        assert np.unique(pd[0][floored]).size == 1
