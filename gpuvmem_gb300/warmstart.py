@@ -325,8 +325,12 @@ def summarize(rows: List[dict]) -> dict:
     tw = np.array([r["t_warm"] for r in ok])
     ok1 = [r for r in rows if r["reached_plain"] and r.get("reached_warm_priors_first")]
     sp1 = [r["t_plain"] / r["t_warm_priors_first"] for r in ok1]
+    tp1 = sum(r["t_plain"] for r in ok1)
+    tw1 = sum(r["t_warm_priors_first"] for r in ok1)
     return {"skies": len(rows), "both_reached": len(ok),
             "speedup_median_priors_first": float(np.median(sp1)) if ok1 else None,
+            "speedup_total_priors_first": float(tp1 / tw1) if ok1 else None,
+            "both_reached_priors_first": len(ok1),
             "warm_chosen": sum(r["start"] == "warm" for r in rows),
             "t_plain_median_s": float(np.median(tp)) if ok else None,
             "t_warm_median_s": float(np.median(tw)) if ok else None,

@@ -146,3 +146,5 @@ def test_summary_counts_only_skies_that_reach_the_target_in_both_runs():
     assert s["it_plain_median"] == 50 and s["it_warm_median"] == 20
     # priors-first: skies 1, 2 and 4 reach it (ratios 4, 2, 300)
     assert s["speedup_median_priors_first"] == pytest.approx(4.0)
+    assert s["both_reached_priors_first"] == 3
+    assert s["speedup_total_priors_first"] == pytest.approx((0.06 + 0.04 + 0.30) / (0.015 + 0.02 + 0.001))
