@@ -346,11 +346,10 @@ struct Workspace {
 // (which forms xt per pixel too); k_ls_step waits for both.  One graph per
 // set of buffers and objective gating, as for the evaluation graphs.
 constexpr int kLsCap = 4096;  // objective evaluations of one search at most
-// evaluations in the WHILE body: an iteration of the loop costs 5.4 us on the
-// GB300 against 0.7 us for a kernel node, so four evaluations share one; the
-// ones after the search's end return at once (1.5 of them a search on
-// average)
-constexpr int kLsUnroll = 4;
+// evaluations in the WHILE body (those after the search's end return at
+// once).  One: with four the loop measured slower (27 against 24.5 us an
+// evaluation at 256^2), as a body's launch costs grow with its nodes.
+constexpr int kLsUnroll = 1;
 
 struct LsEntry {
   const float* pcom;
