@@ -325,10 +325,6 @@ struct XtSource {
   float floor_val;
   float floor_cmp;  // float_below(-eta * minpix): v > floor_cmp as in FP64
   int positivity;
-  // the search's state word (LsState::state): the kernels of an evaluation
-  // that runs after the search has ended (a WHILE body holds several
-  // evaluations) return without an effect; null outside a line search
-  const int* ls_state;
 };
 gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
                       const XtSource* xs = nullptr, double* term_out = nullptr,

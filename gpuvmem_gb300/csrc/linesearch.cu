@@ -3,12 +3,10 @@
 // evaluation k_ls_step advances the state machine of ls_core.cuh (the
 // bracketing step of src/mnbrak.cu:44-98 and Brent's minimiser of
 // src/brent.cu:43-121) and sets the loop condition, so a whole line search
-// is one graph launch with no host round trip per evaluation.  The loop body
-// holds several evaluations (an iteration of the loop costs more than a
-// kernel launch); those after the search's end find the state done and
-// return at once.  The loop ends after `cap` evaluations at the latest (the
-// host bracketing loop has no bound; an unbounded decrease along the line
-// ends here with an error status instead).
+// is one graph launch with no host round trip per evaluation.  The loop ends
+// after `cap` evaluations at the latest (the host bracketing loop has no
+// bound; an unbounded decrease along the line ends here with an error status
+// instead).
 #include "ls_core.cuh"
 
 namespace gv {
@@ -34,12 +32,6 @@ __global__ void k_ls_begin(LsState* s, LsTerms terms, float tol, int cap) {
 
 __global__ void k_ls_step(LsState* s, double* scal, cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0) return;
-  // an evaluation past the end of the search (the loop body holds several)
-  // changes nothing
-  if (__ldcg(&s->state) == ls::kDone) {
-    cudaGraphSetConditional(h, 0u);
-    return;
-  }
   const bool more = ls::ls_step(s, scal);
   cudaGraphSetConditional(h, more ? 1u : 0u);
 }

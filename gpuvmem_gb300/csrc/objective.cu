@@ -180,13 +180,6 @@ __device__ __forceinline__ void xt_pixel(const XtSource& xs, float x, int64_t MN
   xt_value(xs, x, xs.pcom[q], xs.xicom[q], xs.pcom[MN + q], xs.xicom[MN + q], i0, al);
 }
 
-// Whether the line search whose state word is at ls_state has already
-// ended (an evaluation of a WHILE body past the search's end returns
-// without an effect).
-__device__ __forceinline__ bool search_over(const int* ls_state) {
-  return ls_state != nullptr && __ldcg(ls_state) == ls::kDone;
-}
-
 // What clip2IWNoise (src/functions.cu:2694-2719) leaves at one pixel.
 struct ClipRule {
   float clip_i0, threshold;
@@ -307,7 +300,6 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
                     sp.flag_opt};
   const bool from_xt = sp.xs.pcom != nullptr;
   const float x = from_xt ? __ldcg(sp.xs.x_dev) : 0.0f;
-  const bool over = from_xt && search_over(sp.xs.ls_state);
   {
     float i0[VPT], al[VPT];
 #pragma unroll
@@ -323,7 +315,6 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
         }
       }
     }
-    if (over) return;
 #pragma unroll
     for (int k = 0; k < VPT; k++) {
       const int j = threadIdx.x + k * blockDim.x;
@@ -391,13 +382,11 @@ __device__ __forceinline__ float2 phase_rotated(float2 g, float u, float v) {
 template <bool kL2Loads, int VPT>
 __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* __restrict__ rot_u,
                                          const float* __restrict__ rot_v, const float2* tw,
-                                         float2* __restrict__ G, float2* buf, int j0,
-                                         const int* ls_state = nullptr) {
+                                         float2* __restrict__ G, float2* buf, int j0) {
   const int n = N;
   const int lcb = __ffs(cb) - 1;  // cb is a power of two
   // every load of the thread first (cb n <= VPT blockDim.x), then the stores:
-  // the loads are in flight together (with the search's state word)
-  const bool over = search_over(ls_state);
+  // the loads are in flight together
   float2 v[VPT];
 #pragma unroll
   for (int k = 0; k < VPT; k++) {
@@ -407,7 +396,6 @@ __device__ __forceinline__ void col_task(int N, int log2n, int cb, const float* 
       v[k] = kL2Loads ? __ldcg(src) : *src;
     }
   }
-  if (over) return;
 #pragma unroll
   for (int k = 0; k < VPT; k++) {
     const int idx = threadIdx.x + k * blockDim.x;
@@ -431,11 +419,10 @@ __global__ void __launch_bounds__(512, 2) k_cols_fft(int N, int log2n, int64_t M
                                                      const float* __restrict__ rot_u,
                                                      const float* __restrict__ rot_v,
                                                      const float2* __restrict__ tw_g,
-                                                     float2* __restrict__ grid,
-                                                     const int* __restrict__ ls_state) {
+                                                     float2* __restrict__ grid) {
   extern __shared__ float2 sm[];
   col_task<false, kVptLarge>(N, log2n, cb, rot_u, rot_v, tw_g, grid + (int64_t)blockIdx.y * MN, sm,
-                             blockIdx.x * cb, ls_state);
+                  blockIdx.x * cb);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -498,7 +485,6 @@ struct DegridArgs {
   double* __restrict__ term_out;
   uint32_t zero_terms;
   double* __restrict__ term_slots;
-  const int* ls_state;  // the line search's state word, or null
 };
 
 // vis_mod (src/functions.cu:2557-2609): bilinear interpolation of the grid
@@ -536,7 +522,6 @@ __device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, 
   const float2* __restrict__ G = a.grid + (int64_t)c * a.MN;
   const int N = a.N;
   const int nm1 = N - 1;
-  const bool over = search_over(a.ls_state);
   CompSum acc;
   for (int64_t k = b * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
        k += (int64_t)nb * blockDim.x) {
@@ -552,13 +537,12 @@ __device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, 
     float rr, ri;
     vis_residual(d, o, v11, v12, v21, v22, rr, ri);
     acc.add(chi2_term(d.w, rr, ri));
-    if (a.store && !over) {
+    if (a.store) {
       const float2 cv = make_float2(d.w * rr, d.w * ri);
       __stcs(a.cvr + rg.off + k, cv);
       mx = fmaxf(mx, fmaxf(fabsf(cv.x), fabsf(cv.y)));
     }
   }
-  if (over) return false;
   if (a.store) {
     for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, s));
     if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(a.cmax, __float_as_uint(mx));
@@ -710,7 +694,6 @@ __device__ __forceinline__ float prior_grad_pixel(const PriorParams& pp,
 struct PlainImage {
   const float* p;
   __device__ void bind() {}
-  __device__ bool search_done() const { return false; }
   __device__ __forceinline__ float operator[](int64_t q) const { return p[q]; }
 };
 
@@ -721,12 +704,7 @@ struct XtImage {
   ClipRule cr;
   int plane;
   float x;
-  bool over;
-  __device__ void bind() {
-    x = __ldcg(xs.x_dev);
-    over = search_over(xs.ls_state);
-  }
-  __device__ bool search_done() const { return over; }
+  __device__ void bind() { x = __ldcg(xs.x_dev); }
   __device__ __forceinline__ float operator[](int64_t q) const {
     float i0, al;
     xt_pixel(xs, x, MN, q, i0, al);
@@ -746,7 +724,6 @@ struct ClipImage {
   ClipRule cr;
   int plane;
   __device__ void bind() {}
-  __device__ bool search_done() const { return false; }
   __device__ __forceinline__ float operator[](int64_t q) const {
     float i0 = __ldcg(p + q), al = __ldcg(p + MN + q);
     clip_pixel(mask[q], cr, i0, al);
@@ -779,7 +756,6 @@ __device__ __forceinline__ void prior_task(const PriorSet<Img>& ps, const uint8_
     const int i = (int)(q / pp.N), j = (int)(q - (int64_t)i * pp.N);
     acc.add(prior_pixel(pp, I, i, j));
   }
-  if (I.search_done()) return;
   const double bsum = block_sum(acc.value());
   if (threadIdx.x == 0) ps.part[t][b] = bsum;
   if (last_block_done(done, nb * ps.n)) {
@@ -894,9 +870,6 @@ struct FusedArgs {
 template <class Img>
 __global__ void __launch_bounds__(256, 2) k_objective_fused(FusedArgs<Img> f) {
   extern __shared__ float2 sm[];
-  // an evaluation past the end of its line search: every block leaves before
-  // the first grid barrier
-  if (search_over(f.sp.xs.ls_state)) return;
   const int n = f.sp.N;
   float2* buf = sm;  // cb columns, fft_stride(n) apart
   const float2* tw = f.tw;
@@ -1040,7 +1013,7 @@ static StageParams stage_params(const Problem& P, int flag_opt, int write_clip,
   sp.gcf = P.d_gcf;
   sp.beam_x = P.d_beam_x;
   sp.beam_y = P.d_beam_y;
-  sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0f, 0, nullptr};
+  sp.xs = xs ? *xs : XtSource{nullptr, nullptr, nullptr, 0.0f, 0.0f, 0};
   return sp;
 }
 
@@ -1071,8 +1044,7 @@ gv_status model_grids_launch(Problem& P, float* d_img, int flag_opt, int write_c
   if (sm2 > 48 * 1024)
     GV_CUDA(cudaFuncSetAttribute(k_cols_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
   k_cols_fft<<<dim3(n / cb, C), threads2, sm2, P.stream>>>(n, P.log2n, sp.MN, cb, P.d_rot_u,
-                                                           P.d_rot_v, P.d_twiddle, P.d_grid,
-                                                           sp.xs.ls_state);
+                                                           P.d_rot_v, P.d_twiddle, P.d_grid);
   GV_LAUNCH("k_cols_fft");
   return GV_OK;
 }
@@ -1092,8 +1064,7 @@ static DegridArgs degrid_args(Problem& P, bool store_res, double* term_out, uint
   return DegridArgs{P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid, P.d_cvr,
                     store_res ? 1 : 0, P.d_part, P.part_stride, P.d_flags + kFlagCvrMax,
                     P.d_flags + kFlagDegridDone, P.d_chnvis, P.normalize,
-                    P.d_scal + kSlotChi2, term_out, zero_terms, P.d_scal + kSlotTerm0,
-                    nullptr};
+                    P.d_scal + kSlotChi2, term_out, zero_terms, P.d_scal + kSlotTerm0};
 }
 
 static int prior_blocks(const Problem& P) {
@@ -1200,8 +1171,7 @@ gv_status chi2_launch(Problem& P, float* d_img, int flag_opt, bool store_res,
   const int C = (int)P.chans.size();
   const int nb = degrid_blocks(P);
   if (store_res) GV_CUDA(cudaMemsetAsync(P.d_flags + kFlagCvrMax, 0, sizeof(uint32_t), P.stream));
-  DegridArgs da = degrid_args(P, store_res, term_out, zero_terms);
-  da.ls_state = xs ? xs->ls_state : nullptr;
+  const DegridArgs da = degrid_args(P, store_res, term_out, zero_terms);
   k_degrid<<<dim3(nb, C), P.degrid_threads, 0, P.stream>>>(da);
   GV_LAUNCH("k_degrid");
   return GV_OK;

@@ -346,10 +346,6 @@ struct Workspace {
 // (which forms xt per pixel too); k_ls_step waits for both.  One graph per
 // set of buffers and objective gating, as for the evaluation graphs.
 constexpr int kLsCap = 4096;  // objective evaluations of one search at most
-// evaluations in the WHILE body (those after the search's end return at
-// once).  One: with four the loop measured slower (27 against 24.5 us an
-// evaluation at 256^2), as a body's launch costs grow with its nodes.
-constexpr int kLsUnroll = 1;
 
 struct LsEntry {
   const float* pcom;
@@ -426,16 +422,13 @@ gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
   }
   // evaluateXt at the controller's point happens in the FFT staging kernel
   // (and in the prior kernel, which runs beside the Chi2 kernels)
-  const XtSource xs{pcom, xicom, &P.d_ls->x_req, floor_val, floor_cmp, positivity,
-                    &P.d_ls->state};
-  for (int u = 0; u < kLsUnroll && s == GV_OK; u++) {
-    s = ls_objective_launch(P, xt, flag, xs, c.side, c.fork, c.join);
-    if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
-  }
+  const XtSource xs{pcom, xicom, &P.d_ls->x_req, floor_val, floor_cmp, positivity};
+  s = ls_objective_launch(P, xt, flag, xs, c.side, c.fork, c.join);
+  if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
   cudaGraph_t g2 = body;
   e = cudaStreamEndCapture(c.cap, &g2);
   P.stream = saved;
-  *body_launches = (gv_launch_count() - l1) / kLsUnroll;  // one evaluation's
+  *body_launches = gv_launch_count() - l1;
   add_launches(-(gv_launch_count() - l0));  // counted again at each replay
   if (s != GV_OK) return s;
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (line search body)");
@@ -710,8 +703,7 @@ class Solver {
     GV_TRY(fetch_scalars(P_, kSlotLs + 4));
     const int64_t evals = (int64_t)P_.h_scal[kSlotLs + 1];
     n_obj_ += evals;
-    // the WHILE body runs whole: kLsUnroll evaluations an iteration
-    add_launches(1 + (evals + kLsUnroll - 1) / kLsUnroll * kLsUnroll * hit->body_launches);
+    add_launches(1 + evals * hit->body_launches);
     *fret = (float)P_.h_scal[kSlotLs];
     if (P_.h_scal[kSlotLs + 2] != 0.0) {
       set_error("line search did not end within its evaluation limit (unbounded along the line?)");
