@@ -86,11 +86,17 @@ constexpr int kDH = kDW / 4;        // drain warps per lane quarter (column slic
 constexpr int kThreads = (kGW + kDW + 2) * 32;
 constexpr int kVPL = 2;             // visibilities per generator lane (packed FP32x2 chains)
 constexpr int kVisSlots = 6;
-// default chunks accumulated before a drain: at 2048^2 x 35.28M
-// visibilities 4 / 8 / 16 chunks give 1.30 / 1.245 / 1.23 s a gradient and
-// 1.1e-6 / 4.1e-6 / 7.4e-6 of max|grad| off the FP64 oracle (the gate is
-// 1e-5; the reference's own kernel is 7.5e-4 off)
-constexpr int kSlab = 8;
+// default chunks accumulated before a drain: 8 where a split holds at least
+// kSlabLongSplit chunks, else 4.  At 2048^2 x 35.28M visibilities (about 20K
+// chunks a split) 4 / 8 / 16 chunks give 1.30 / 1.245 / 1.23 s a gradient
+// and 1.1e-6 / 4.1e-6 / 7.4e-6 of max|grad| off the FP64 oracle (the gate is
+// 1e-5; the reference's own kernel is 7.5e-4 off).  At 256^2 x 104,400 (44
+// chunks a split) the drain costs little, and 8 chunks would put the
+// gradient 1.05e-5 of max|grad| from the reference's own (which is itself
+// 8.1e-6 off the oracle; ours 2.8e-6 at 8, 1.5e-6 at 4).
+constexpr int kSlab = 4;
+constexpr int kSlabLong = 8;
+constexpr int64_t kSlabLongSplit = 1024;
 constexpr uint32_t kTmemCols = 512;
 
 struct VisEntry {
@@ -880,7 +886,10 @@ gv_status dchi2_tc(Problem& P, const float* d_img, int flag_opt, float* d_result
   p.fast_anchor = P.tc_fast_anchor;
   {
     const char* sl = std::getenv("GV_TC_SLAB");
-    p.slab = sl ? std::max(1, std::atoi(sl)) : tc::kSlab;
+    const int64_t vis = only_channel >= 0 ? P.chans[only_channel].ngrid : P.Vgrid;
+    const int64_t chunks_per_split = vis / std::max(1, P.tc_nsplit) / tc::kChunkVis;
+    p.slab = sl ? std::max(1, std::atoi(sl))
+                : (chunks_per_split >= tc::kSlabLongSplit ? tc::kSlabLong : tc::kSlab);
   }
   const int TN = tc_tile_n(P);
   const bool pair = tc_pair(P);

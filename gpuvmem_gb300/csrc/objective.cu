@@ -523,10 +523,23 @@ __device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, 
   const int N = a.N;
   const int nm1 = N - 1;
   CompSum acc;
-  for (int64_t k = b * (int64_t)blockDim.x + threadIdx.x; k < rg.ngrid;
-       k += (int64_t)nb * blockDim.x) {
-    const float4 d = __ldcs(a.deg + rg.off + k);
-    const float2 o = __ldcs(a.vo + rg.off + k);
+  // the next visibility's record and Vo are loaded before this one's grid
+  // cells are gathered, so the stream's latency overlaps the gathers
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  int64_t k = b * (int64_t)blockDim.x + threadIdx.x;
+  float4 d_next = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float2 o_next = make_float2(0.0f, 0.0f);
+  if (k < rg.ngrid) {
+    d_next = __ldcs(a.deg + rg.off + k);
+    o_next = __ldcs(a.vo + rg.off + k);
+  }
+  for (; k < rg.ngrid; k += stride) {
+    const float4 d = d_next;
+    const float2 o = o_next;
+    if (k + stride < rg.ngrid) {
+      d_next = __ldcs(a.deg + rg.off + k + stride);
+      o_next = __ldcs(a.vo + rg.off + k + stride);
+    }
     const uint32_t cell = __float_as_uint(d.x);
     const int i1 = cell & 0xffff, j1 = cell >> 16;
     const int i2 = (i1 + 1) & nm1, j2 = (j1 + 1) & nm1;
