@@ -15,10 +15,13 @@
 //
 // The FFT passes are radix-8 Stockham passes in shared memory with the
 // butterflies in registers (four passes and barriers for a 2048-point line
-// instead of eleven radix-2 stages).  Images up to 512 x 512 run the three
-// passes and the prior values as one cooperative launch
-// (k_objective_fused).  No per-call allocation, no host synchronisation
-// except the single scalar read-back at the end of an evaluation.
+// instead of eleven radix-2 stages).  With GV_FUSED=1 at creation, images
+// up to 512 x 512 run the three passes and the prior values as one
+// cooperative launch (k_objective_fused; bit-identical, but slower on the
+// GB300 than the separate launches, whose kernel nodes cost 0.7 us against
+// about 2 us for a grid-wide barrier).  No per-call allocation, no host
+// synchronisation except the single scalar read-back at the end of an
+// evaluation.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
