@@ -159,7 +159,7 @@ def measured_peaks():
 # visibilities).  The traffic of the full launch is this times its
 # visibilities: the operands are generated on chip, so the traffic is the
 # visibility constants re-read per output tile plus the partial images.
-DCHI2_DRAM_BYTES_PER_VIS = 168.43
+DCHI2_DRAM_BYTES_PER_VIS = 168.48
 DCHI2_TRAFFIC_SOURCE = ("ncu capture of k_dchi2_tc, one channel of 2048^2 (bench.py --case "
                         "dchi2_2048_1ch), scaled by the visibility count")
 
