@@ -211,24 +211,45 @@ __device__ __forceinline__ float beam_arc(float x, float y) {
   return sqrtf(__fmaf_rn(x, x, __fmul_rn(y, y)));
 }
 
-__device__ inline float attenuation_arc(float arc, float freq, float D, float pbf, float cutoff,
-                                        int pb) {
-  const float lambda = wavelength(freq);
+// attenuation_arc's per-frequency constants, taken once per channel by
+// callers staging many pixels: the same operations in the same order, so
+// the same values.
+struct BeamAt {
+  float lambda, fwhm, c, krz_pbf, D, cutoff;
+  int pb;
+};
+
+__device__ __forceinline__ BeamAt beam_at(float freq, float D, float pbf, float cutoff, int pb) {
+  BeamAt b;
+  b.lambda = wavelength(freq);
+  b.fwhm = pbf * b.lambda / D;
+  b.c = 4.0f * logf(2.0f);
+  b.krz_pbf = kRZ / pbf;
+  b.D = D;
+  b.cutoff = cutoff;
+  b.pb = pb;
+  return b;
+}
+
+__device__ __forceinline__ float attenuation_at(float arc, const BeamAt& b) {
   float atten;
-  if (pb == GV_BEAM_GAUSSIAN) {
-    const float fwhm = pbf * lambda / D;
-    const float c = 4.0f * logf(2.0f);
-    const float r = arc / fwhm;
-    atten = expf(-c * r * r);
+  if (b.pb == GV_BEAM_GAUSSIAN) {
+    const float r = arc / b.fwhm;
+    atten = expf(-b.c * r * r);
   } else {
     atten = 1.0f;
     if (arc != 0.0f) {
-      const float arg = kPiF * arc * D / lambda * (kRZ / pbf);
-      const float b = j1f(arg);
-      atten = 4.0f * (b / arg) * (b / arg);
+      const float arg = kPiF * arc * b.D / b.lambda * b.krz_pbf;
+      const float bj = j1f(arg);
+      atten = 4.0f * (bj / arg) * (bj / arg);
     }
   }
-  return arc <= cutoff ? atten : 0.0f;
+  return arc <= b.cutoff ? atten : 0.0f;
+}
+
+__device__ inline float attenuation_arc(float arc, float freq, float D, float pbf, float cutoff,
+                                        int pb) {
+  return attenuation_at(arc, beam_at(freq, D, pbf, cutoff, pb));
 }
 
 __device__ inline float attenuation_xy(float x, float y, float freq, float D, float pbf,

@@ -218,10 +218,11 @@ struct StageParams {
 // (src/functions.cu:2424-2444) at beam radius arc, fg_scale, and apply_GCF
 // (src/functions.cu:2468) when a correction is set.
 __device__ __forceinline__ float stage_value(const StageParams& sp, float i0, float al, float arc,
-                                             float freq, float nudiv, float floor_inu, int64_t q) {
+                                             const BeamAt& beam, float nudiv, float floor_inu,
+                                             int64_t q) {
   float inu = i0 * (al == 0.0f ? 1.0f : powf(nudiv, al));
   if (inu < floor_inu) inu = floor_inu;
-  const float a = attenuation_arc(arc, freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
+  const float a = attenuation_at(arc, beam);
   float v = inu * a * sp.fg_scale;
   if (sp.gcf) v *= sp.gcf[q];
   return v;
@@ -344,6 +345,7 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
   for (int c = 0; c < C; c++) {
     const float freq = chfreq[c];
     const float nudiv = freq / sp.nu_0;
+    const BeamAt beam = beam_at(freq, sp.D, sp.pbf, sp.pbcut, sp.pb);
     // unrolled by two only: the transcendental functions of many pixels at
     // once would raise the register count and lower the occupancy
 #pragma unroll 2
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float
       const int j = threadIdx.x + k * blockDim.x;
       if (j < n) {
         buf[fpad(j)] = make_float2(
-            stage_value(sp, s_i0[j], s_al[j], s_arc[j], freq, nudiv, floor_inu, (int64_t)n * i + j),
+            stage_value(sp, s_i0[j], s_al[j], s_arc[j], beam, nudiv, floor_inu, (int64_t)n * i + j),
             0.0f);
       }
     }
