@@ -289,11 +289,10 @@ __device__ __forceinline__ void row_task(const StageParams& sp, const float* __r
 // grid.  The same arithmetic per pixel and channel as row_task.  VPT: the
 // row's values per thread (n / blockDim.x, at least 2).
 template <int VPT>
-__global__ void __launch_bounds__(256, 3) k_rows_fft(StageParams sp, const float* __restrict__ chfreq,
-                                                  int C, float* __restrict__ img,
-                                                  const uint8_t* __restrict__ mask,
-                                                  const float2* __restrict__ tw,
-                                                  float2* __restrict__ grid) {
+__global__ void __launch_bounds__(256, VPT >= 16 ? 3 : 4)
+    k_rows_fft(StageParams sp, const float* __restrict__ chfreq, int C, float* __restrict__ img,
+               const uint8_t* __restrict__ mask, const float2* __restrict__ tw,
+               float2* __restrict__ grid) {
   extern __shared__ float2 buf[];  // the row (fft_span(n)), its clipped I_nu0, alpha, beam radius
   const int n = sp.N, i = blockIdx.x;
   float* s_i0 = reinterpret_cast<float*>(buf + fft_span(n));
