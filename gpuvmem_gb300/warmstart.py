@@ -344,12 +344,15 @@ def main(argv: Optional[Sequence[str]] = None):
     """Trains and evaluates the warm start.  The network shipped in
     gpuvmem_gb300/data/warmstart_unet.npz was made by
 
-        python -m gpuvmem_gb300.warmstart --train 2000 --eval 200 --epochs 40 \
-            --shapes 4x32,5x16 --save gpurun_out/unet_{shape}.npz --out gpurun_out/ws.json
+        python -m gpuvmem_gb300.warmstart --train 2000 --eval 200 --epochs 80 \
+            --shapes 5x16 --pair-iterations 300 \
+            --save gpurun_out/unet_{shape}_p300e80.npz --out gpurun_out/ws_p300e80.json
 
-    (pairs from the plain solver on seeds 1000-2999, the held-out skies are
-    seeds 900000-900199), keeping the shape with the larger summed-time
-    speed-up."""
+    (pairs from the plain solver on seeds 1000-2999, each solved for up to
+    300 iterations as the evaluation's plain runs are; the held-out skies
+    are seeds 900000-900199).  The 5-level shape was chosen over the planned
+    4 x 32 by an earlier run of both shapes on the same pairs
+    (`--shapes 4x32,5x16`), which kept the larger summed-time speed-up."""
     ap = argparse.ArgumentParser(description="train and evaluate the learned warm start")
     ap.add_argument("--train", type=int, default=512)
     ap.add_argument("--eval", type=int, default=32)
