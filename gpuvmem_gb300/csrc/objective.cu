@@ -34,13 +34,13 @@ namespace gv {
 
 namespace {
 
-
 // The arithmetic that more than one kernel performs on the same values (the
 // FFT butterflies and twiddles, the phase rotation, the degridding's model
 // and chi2 terms, the prior stencils) spells out every multiply-add with
-// rounding intrinsics: the compiler never contracts those, so a separate
-// kernel, a fused one and the cluster line search round each operation
-// alike wherever the code is inlined.
+// rounding intrinsics: the compiler never contracts those, so the separate
+// kernels and the fused ones round each operation alike wherever the code
+// is inlined (the compiler's choice of which product to fuse into an FMA
+// can otherwise differ between inlining contexts).
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)),
                      __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
@@ -517,10 +517,10 @@ __device__ __forceinline__ float chi2_term(float w, float rr, float ri) {
 // Pass 3 for block b of nb of channel c: vis_mod + residual + chi2Vector
 // over the block's share of the cell-sorted visibilities and the block's
 // FP64 partial; the last of the nb * C blocks to finish adds the partials
-// into the chi2 scalar (and returns true).  kL2Loads: read the grid from L2
-// (written earlier in the same kernel by other blocks).
+// into the chi2 scalar.  kL2Loads: read the grid from L2 (written earlier in
+// the same kernel by other blocks).
 template <bool kL2Loads>
-__device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
+__device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
   float mx = 0.0f;
   const ChanRange rg = a.ranges[c];
   const float2* __restrict__ G = a.grid + (int64_t)c * a.MN;
@@ -575,9 +575,7 @@ __device__ __forceinline__ bool degrid_task(const DegridArgs& a, int b, int nb, 
       for (int t = 0; t < 32; t++)
         if (a.zero_terms & (1u << t)) a.term_slots[t] = 0.0;
     }
-    return true;
   }
-  return false;
 }
 
 // Pass 3: vis_mod + residual + chi2Vector + partial reduction; the last
