@@ -1,9 +1,9 @@
 // linmin's line search (src/linmin.cu:52-110) on the GPU: the bracketing
 // step (src/mnbrak.cu:44-98) and Brent's minimiser (src/brent.cu:43-121) as
 // a state machine in device memory, advanced by one thread after every
-// objective evaluation.  Included by the graph-loop controller
-// (linesearch.cu) and by the single-launch line search of small images
-// (objective.cu).
+// objective evaluation (k_ls_step of the CUDA-graph loop, linesearch.cu).
+// Kept in a header of its own so any kernel that steps the search shares
+// this code.
 //
 // The arithmetic is the host version's, operation for operation: float
 // variables, and the double-precision constants (GOLD 1.618034, GLIMIT 100,
@@ -36,7 +36,6 @@ enum LsWait {
   kWaitFu,      // Brent: f(u)
   kDone
 };
-
 
 // Takes f at the point last asked for and advances; returns true when it asks
 // for another evaluation (at s.x_req), false when the search is over.

@@ -28,7 +28,6 @@
 #include <cstring>
 
 #include "gv_internal.cuh"
-#include "ls_core.cuh"
 
 namespace gv {
 
