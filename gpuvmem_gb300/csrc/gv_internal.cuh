@@ -364,8 +364,12 @@ gv_status batch_objective_args(Problem& P, float* d_img, int flag_opt, void* out
 gv_status batch_objective_launch(int np, const void* d_args, const int* d_off, int max_n,
                                  int max_tasks, uint32_t* d_bar, uint32_t* d_err, int num_sms,
                                  cudaStream_t st);
+// With ls set (no fused launch, a degridding grid resident at once) the
+// degridding's last block also takes the search's step and sets the loop
+// condition cond (*stepped = true); otherwise the caller adds the step.
 gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
-                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, LsState* ls,
+                              cudaGraphConditionalHandle cond, bool* stepped);
 gv_status fetch_scalars(Problem& P, int n);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);

@@ -28,6 +28,7 @@
 #include <cstring>
 
 #include "gv_internal.cuh"
+#include "ls_core.cuh"
 
 namespace gv {
 
@@ -488,7 +489,21 @@ struct DegridArgs {
   double* __restrict__ term_out;
   uint32_t zero_terms;
   double* __restrict__ term_slots;
+  // k_degrid_ls: the block that sums chi2 also takes the search's step
+  // and sets the graph's loop condition
+  LsState* ls;
+  double* ls_scal;
+  cudaGraphConditionalHandle ls_cond;
 };
+
+// the search's step, on the state where it lies in global memory (the
+// previous evaluation's kernels wrote it; one thread reads and writes it
+// here), so the degridding keeps its registers
+__device__ __forceinline__ void degrid_ls_step(LsState* ls, double* scal,
+                                               cudaGraphConditionalHandle h) {
+  const bool more = ls::ls_step_on(*ls, scal);
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
 
 // vis_mod (src/functions.cu:2557-2609): bilinear interpolation of the grid
 // at the visibility's fractional cell offsets (d.y, d.z) from the four cell
@@ -518,7 +533,7 @@ __device__ __forceinline__ float chi2_term(float w, float rr, float ri) {
 // FP64 partial; the last of the nb * C blocks to finish adds the partials
 // into the chi2 scalar.  kL2Loads: read the grid from L2 (written earlier in
 // the same kernel by other blocks).
-template <bool kL2Loads>
+template <bool kL2Loads, bool kStep = false>
 __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, int c, int C) {
   float mx = 0.0f;
   const ChanRange rg = a.ranges[c];
@@ -573,6 +588,7 @@ __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, 
       if (a.term_out) *a.term_out = *a.chi2_out;
       for (int t = 0; t < 32; t++)
         if (a.zero_terms & (1u << t)) a.term_slots[t] = 0.0;
+      if (kStep) degrid_ls_step(a.ls, a.ls_scal, a.ls_cond);
     }
   }
 }
@@ -581,6 +597,12 @@ __device__ __forceinline__ void degrid_task(const DegridArgs& a, int b, int nb, 
 // block to finish adds the partials into the chi2 scalar.
 __global__ void __launch_bounds__(256) k_degrid(DegridArgs a) {
   degrid_task<false>(a, blockIdx.x, gridDim.x, blockIdx.y, gridDim.y);
+}
+
+// The same inside the line search's graph loop: the last block also steps
+// the search and sets the loop's condition.
+__global__ void __launch_bounds__(256) k_degrid_ls(DegridArgs a) {
+  degrid_task<false, true>(a, blockIdx.x, gridDim.x, blockIdx.y, gridDim.y);
 }
 
 // ---- priors ---------------------------------------------------------------
@@ -1078,7 +1100,8 @@ static DegridArgs degrid_args(Problem& P, bool store_res, double* term_out, uint
   return DegridArgs{P.N, MN, P.d_ranges, P.d_deg, P.d_vo, P.d_grid, P.d_cvr,
                     store_res ? 1 : 0, P.d_part, P.part_stride, P.d_flags + kFlagCvrMax,
                     P.d_flags + kFlagDegridDone, P.d_chnvis, P.normalize,
-                    P.d_scal + kSlotChi2, term_out, zero_terms, P.d_scal + kSlotTerm0};
+                    P.d_scal + kSlotChi2, term_out, zero_terms, P.d_scal + kSlotTerm0,
+                    nullptr, nullptr, 0};
 }
 
 static int prior_blocks(const Problem& P) {
@@ -1376,9 +1399,14 @@ gv_status objective_launch(Problem& P, float* d_img, int flag_opt, bool store_re
 // the Chi2 kernels on P.stream (the staging kernel forms xt and writes it
 // to d_xt), the active priors in one launch on `side`, forked from P.stream
 // through `fork` and joined back through `join`; the priors form xt
-// themselves, so both branches run at once.
+// themselves, so both branches run at once.  With `ls` (and a degridding
+// grid that is resident at once) the degridding runs after the join and its
+// last block also steps the search: one kernel node fewer per evaluation in
+// the graph's loop (*stepped = true).
 gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSource& xs,
-                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                              cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, LsState* ls,
+                              cudaGraphConditionalHandle cond, bool* stepped) {
+  *stepped = false;
   int ichi2 = -1;
   uint32_t zero = 0u;
   for (size_t t = 0; t < P.terms.size(); t++) {
@@ -1414,9 +1442,34 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
     if (s != GV_OK) return s;
     GV_CUDA(cudaEventRecord(join, side));
   }
-  gv_status s = chi2_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero);
+  // k_degrid_ls holds more registers than k_degrid (fewer resident blocks):
+  // it is taken only when its whole grid is resident at once, where the
+  // node it saves is worth more (256^2, one channel: 25.1 against 25.7 us
+  // per evaluation) than the latency hiding it gives up (2048^2, eight
+  // channels: 944 against 938 us)
+  const int C = (int)P.chans.size();
+  const int nb = degrid_blocks(P);
+  int resident = 0;
+  GV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_degrid_ls,
+                                                        P.degrid_threads, 0));
+  if (ls == nullptr || (int64_t)nb * C > (int64_t)resident * P.num_sms) {
+    gv_status s = chi2_launch(P, d_xt, flag_opt, false, &xs, P.d_scal + kSlotTerm0 + ichi2, zero);
+    if (s != GV_OK) return s;
+    if (ps.n > 0) GV_CUDA(cudaStreamWaitEvent(P.stream, join, 0));
+    return GV_OK;
+  }
+  gv_status s = model_grids_launch(P, d_xt, flag_opt, 1, &xs);
   if (s != GV_OK) return s;
+  // the degridding waits for the prior values too: its last block adds the
+  // terms up and steps the search
   if (ps.n > 0) GV_CUDA(cudaStreamWaitEvent(P.stream, join, 0));
+  DegridArgs da = degrid_args(P, false, P.d_scal + kSlotTerm0 + ichi2, zero);
+  da.ls = ls;
+  da.ls_scal = P.d_scal;
+  da.ls_cond = cond;
+  k_degrid_ls<<<dim3(nb, C), P.degrid_threads, 0, P.stream>>>(da);
+  GV_LAUNCH("k_degrid_ls");
+  *stepped = true;
   return GV_OK;
 }
 

@@ -423,8 +423,9 @@ gv_status build_ls_graph(Problem& P, LsCache& c, int64_t MN, const float* pcom,
   // evaluateXt at the controller's point happens in the FFT staging kernel
   // (and in the prior kernel, which runs beside the Chi2 kernels)
   const XtSource xs{pcom, xicom, &P.d_ls->x_req, floor_val, floor_cmp, positivity};
-  s = ls_objective_launch(P, xt, flag, xs, c.side, c.fork, c.join);
-  if (s == GV_OK) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
+  bool stepped = false;
+  s = ls_objective_launch(P, xt, flag, xs, c.side, c.fork, c.join, P.d_ls, h, &stepped);
+  if (s == GV_OK && !stepped) s = ls_step_launch(c.cap, P.d_ls, P.d_scal, h);
   cudaGraph_t g2 = body;
   e = cudaStreamEndCapture(c.cap, &g2);
   P.stream = saved;
