@@ -18,8 +18,6 @@
 //
 // The tables are host arithmetic in FP32 with the C library's sqrtf, expf,
 // powf and sinf, as the reference computes them on the host.
-#include <cub/cub.cuh>
-
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -470,15 +468,9 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
   GV_CUDA(cudaMalloc(&b.ktab, sizeof(float) * kernel->m * kernel->n));
   GV_CUDA(cudaMemcpyAsync(b.ktab, kernel->values, sizeof(float) * kernel->m * kernel->n,
                           cudaMemcpyHostToDevice, st));
-  size_t sort_bytes = 0, scan_bytes = 0, rle_bytes = 0, rscan_bytes = 0;
-  GV_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, b.keys, b.skeys, b.slots, b.sslots,
-                                          (int)kcap, 0, cellbits, st));
-  GV_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, b.flag, b.pos, (int)MN, st));
-  GV_CUDA(cub::DeviceRunLengthEncode::Encode(nullptr, rle_bytes, b.skeys, b.rcell, b.rcount,
-                                             b.nruns, (int)kcap, st));
-  GV_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, rscan_bytes, b.rcount, b.rstart, (int)rcap, st));
   const size_t tmp_bytes =
-      std::max(std::max(sort_bytes, scan_bytes), std::max(rle_bytes, rscan_bytes));
+      std::max(std::max(radix_sort_scratch<uint32_t, uint32_t>(kcap), scan_scratch(MN)),
+               rle_scratch(kcap));
   GV_CUDA(cudaMalloc(&b.tmp, tmp_bytes));
   for (int c = 0; c < nchannels; c++) {
     const int64_t n = in[c].nvis;
@@ -499,18 +491,12 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
       GV_LAUNCH("k_grid_cells");
       k_grid_keys<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(g, nk, b.base, b.keys, b.slots);
       GV_LAUNCH("k_grid_keys");
-      size_t tb = tmp_bytes;
-      GV_CUDA(cub::DeviceRadixSort::SortPairs(b.tmp, tb, b.keys, b.skeys, b.slots, b.sslots,
-                                              (int)nk, 0, cellbits, st));
-      tb = tmp_bytes;
-      GV_CUDA(cub::DeviceRunLengthEncode::Encode(b.tmp, tb, b.skeys, b.rcell, b.rcount, b.nruns,
-                                                 (int)nk, st));
-      // run starts: exclusive sum of the run lengths (over the capacity; the
-      // entries past the run count are not read)
+      GV_TRY((radix_sort_pairs<uint32_t, uint32_t>(b.tmp, tmp_bytes, b.keys, b.skeys, b.slots,
+                                                    b.sslots, nk, 0, cellbits, st)));
+      // runs of equal cells: cell, first position and length of each
+      GV_TRY(run_length_encode(b.tmp, tmp_bytes, b.skeys, nk, b.rcell, b.rstart, b.rcount, rcap,
+                               b.nruns, st));
       const int64_t nr_cap = std::min<int64_t>(nk, rcap);
-      tb = tmp_bytes;
-      GV_CUDA(cub::DeviceScan::ExclusiveSum(b.tmp, tb, b.rcount, b.rstart, (int)nr_cap, st));
-      add_launches(3);
       const unsigned rb = (unsigned)std::min<int64_t>((nr_cap + kRunWarps - 1) / kRunWarps,
                                                       (int64_t)65535 * 16);
       k_grid_runs<<<rb, kRunWarps * 32, 0, st>>>(g, n, z0, b.rcell, b.rstart, b.rcount, b.nruns,
@@ -521,9 +507,7 @@ extern "C" gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t 
     const unsigned gb = (unsigned)((MN + 255) / 256);
     k_grid_finish<<<gb, 256, 0, st>>>(MN, b.gw, b.gaux, b.gvo, b.flag);
     GV_LAUNCH("k_grid_finish");
-    size_t tb = tmp_bytes;
-    GV_CUDA(cub::DeviceScan::ExclusiveSum(b.tmp, tb, b.flag, b.pos, (int)MN, st));
-    add_launches(1);
+    GV_TRY(exclusive_scan<int>(b.tmp, tmp_bytes, b.flag, b.pos, MN, st));
     k_grid_compact<<<gb, 256, 0, st>>>(g, MN, b.gw, b.gvo, b.flag, b.pos, b.ouvw, b.ovo, b.ow);
     GV_LAUNCH("k_grid_compact");
     int last[2] = {0, 0};

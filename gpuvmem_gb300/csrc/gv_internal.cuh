@@ -371,6 +371,22 @@ gv_status ls_objective_launch(Problem& P, float* d_xt, int flag_opt, const XtSou
                               cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, LsState* ls,
                               cudaGraphConditionalHandle cond, bool* stepped);
 gv_status fetch_scalars(Problem& P, int n);
+
+// Device-wide sort / scan / run-length primitives (sortscan.cu).  Scratch
+// sizes first, then the call; nothing is allocated inside.
+template <class K, class V>
+size_t radix_sort_scratch(int64_t n);
+template <class K, class V>
+gv_status radix_sort_pairs(void* scratch, size_t bytes, const K* kin, K* kout, const V* vin,
+                           V* vout, int64_t n, int begin_bit, int end_bit, cudaStream_t st);
+size_t scan_scratch(int64_t n);
+template <class T>
+gv_status exclusive_scan(void* scratch, size_t bytes, const T* in, T* out, int64_t n,
+                         cudaStream_t st);
+size_t rle_scratch(int64_t n);
+gv_status run_length_encode(void* scratch, size_t bytes, const uint32_t* keys, int64_t n,
+                            uint32_t* rkey, uint32_t* rstart, uint32_t* rcount, int64_t cap,
+                            int* nruns, cudaStream_t st);
 gv_status dchi2_launch(Problem& P, const float* d_img, int flag_opt, float* d_result);
 gv_status dchi2_channel_launch(Problem& P, int c, float* d_out);
 gv_status gradient_launch(Problem& P, float* d_img, float* d_xi, int iter, int flag_opt);

@@ -11,7 +11,6 @@
 //    are then sorted by grid cell so the degridding gathers hit L2 in order.
 //  * total_attenuation / weight_image / noise_image, fg_scale = min(noise),
 //    noise_cut = factor * min(noise) (src/mfs.cu:849-916).
-#include <cub/cub.cuh>
 
 #include <algorithm>
 #include <cmath>
@@ -500,11 +499,16 @@ gv_status setup_problem(Problem& P, const gv_problem_desc& d) {
       P.sum_weights = sum_w;
       P.vis_noise = d.vis_noise > 0.0f ? d.vis_noise : 0.5f * sqrtf(variance);
     }
-    GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, idx,
-                                                  P.d_perm, (int64_t)V, 0, 64, st));
+    tmp_bytes = radix_sort_scratch<unsigned long long, int64_t>((int64_t)V);
     GV_SETUP_CUDA(cudaMalloc(&tmp, tmp_bytes));
-    GV_SETUP_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, idx,
-                                                  P.d_perm, (int64_t)V, 0, 64, st));
+    {
+      const gv_status s = radix_sort_pairs<unsigned long long, int64_t>(
+          tmp, tmp_bytes, keys, keys2, idx, P.d_perm, (int64_t)V, 0, 64, st);
+      if (s != GV_OK) {
+        cleanup();
+        return s;
+      }
+    }
     GV_SETUP_CUDA(cudaMalloc(&P.d_deg, sizeof(float4) * V));
     GV_SETUP_CUDA(cudaMalloc(&P.d_vo, sizeof(float2) * V));
     GV_SETUP_CUDA(cudaMalloc(&P.d_ph, sizeof(uint4) * V));

@@ -15,7 +15,6 @@
 // keep the reference's sequential FP32 order: the sum of the weights on the
 // host (std::accumulate order), the sum of squares of the half grid by one
 // GPU thread.
-#include <cub/cub.cuh>
 
 #include <algorithm>
 #include <cmath>
@@ -181,8 +180,7 @@ extern "C" gv_status gv_apply_weighting(int32_t scheme, float robust, int32_t M,
   GV_CUDA(cudaMalloc(&b.sidx, sizeof(uint32_t) * vmax));
   GV_CUDA(cudaMalloc(&b.grid, sizeof(float) * MN));
   GV_CUDA(cudaMalloc(&b.acc, sizeof(float)));
-  GV_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, b.tmp_bytes, b.key, b.skey, b.idx, b.sidx,
-                                          (int)vmax, 0, 32, st));
+  b.tmp_bytes = radix_sort_scratch<uint32_t, uint32_t>(vmax);
   GV_CUDA(cudaMalloc(&b.tmp, b.tmp_bytes));
   // grid one channel's weights into b.grid (added to what it holds)
   auto grid_channel = [&](int c) -> gv_status {
@@ -193,9 +191,8 @@ extern "C" gv_status gv_apply_weighting(int32_t scheme, float robust, int32_t M,
     const unsigned gb = (unsigned)((n + 255) / 256);
     k_weight_cells<<<gb, 256, 0, st>>>(n, b.uvw, ch[c].freq_hz, adu, adv, M, N, b.key, b.idx);
     GV_LAUNCH("k_weight_cells");
-    size_t tb = b.tmp_bytes;
-    GV_CUDA(cub::DeviceRadixSort::SortPairs(b.tmp, tb, b.key, b.skey, b.idx, b.sidx, (int)n, 0, 32,
-                                            st));
+    GV_TRY((radix_sort_pairs<uint32_t, uint32_t>(b.tmp, b.tmp_bytes, b.key, b.skey, b.idx,
+                                                  b.sidx, n, 0, 32, st)));
     k_cell_runs<<<gb, 256, 0, st>>>(n, b.skey, b.sidx, b.w, b.grid);
     GV_LAUNCH("k_cell_runs");
     return GV_OK;

@@ -380,6 +380,30 @@ gv_status gv_grid_visibilities(const gv_grid_kernel* kernel, int32_t M, int32_t 
                                double deltax_deg, double deltay_deg, int32_t nchannels,
                                const gv_channel_desc* in, gv_channel_desc* out, void* stream);
 
+/* Device sort and scan of the set-up passes (the reference sorts nothing
+ * on the GPU; its gridding walks the visibilities on the host).  The
+ * gridding, the weighting schemes and the visibility ordering of
+ * gv_problem_create use these; they are exported for tests and tools.
+ * Device pointers; work is enqueued on `stream` and the call returns after
+ * it has finished (scratch is allocated and freed inside).
+ * gv_radix_sort_pairs_*: stable sort of (key, value) pairs by the key bits
+ * [begin_bit, end_bit), least significant digit first; keys and values move
+ * whole.  Output buffers must not overlap the inputs.  n < 2^32.
+ * gv_exclusive_scan_i32: out[i] = in[0] + ... + in[i-1] (out may be in).
+ * gv_run_length_encode_u32: runs of equal keys in d_keys: key, first
+ * position and length of each run (at most cap runs are written), and the
+ * run count in *d_nruns (device int). */
+gv_status gv_radix_sort_pairs_u32(const uint32_t* d_keys_in, uint32_t* d_keys_out,
+                                  const uint32_t* d_vals_in, uint32_t* d_vals_out, int64_t n,
+                                  int32_t begin_bit, int32_t end_bit, void* stream);
+gv_status gv_radix_sort_pairs_u64(const uint64_t* d_keys_in, uint64_t* d_keys_out,
+                                  const int64_t* d_vals_in, int64_t* d_vals_out, int64_t n,
+                                  int32_t begin_bit, int32_t end_bit, void* stream);
+gv_status gv_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
+gv_status gv_run_length_encode_u32(const uint32_t* d_keys, int64_t n, uint32_t* d_run_keys,
+                                   uint32_t* d_run_starts, uint32_t* d_run_lengths, int64_t cap,
+                                   int32_t* d_nruns, void* stream);
+
 /* Autotuner (the reference takes its launch shapes from the -X/-Y/-V
  * flags, src/main.cu; here they are measured): times the candidates of the
  * tensor-core DChi2 launch (CTA pairs or single CTAs x split-K counts) and of
