@@ -84,7 +84,8 @@ void* batch_tables(gv_batch* b, const std::vector<float*>& img, int flag, int* m
   const int n = (int)b->probs.size();
   *st = GV_OK;
   if (!b->fused_objective) return nullptr;
-  const size_t ab = (gv::batch_arg_bytes() + 15) / 16 * 16;
+  // the kernel indexes the arguments as an array: the stride is their size
+  const size_t ab = gv::batch_arg_bytes();
   std::vector<unsigned char> host(ab * n + sizeof(int) * 3 * (n + 1) + 16, 0);
   int* off = reinterpret_cast<int*>(host.data() + ab * n);
   *max_n = 0;
@@ -219,7 +220,7 @@ gv_status gv_batch_evaluate(gv_batch* b, float* const* d_imgs, float* const* d_x
       GV_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
       gv_status s = GV_OK;
       if (tables) {
-        const size_t ab = (gv::batch_arg_bytes() + 15) / 16 * 16;
+        const size_t ab = gv::batch_arg_bytes();
         unsigned char* t = static_cast<unsigned char*>(tables);
         const int* d_off = reinterpret_cast<const int*>(t + ab * n);
         uint32_t* d_bar = reinterpret_cast<uint32_t*>(t + ab * n + sizeof(int) * 3 * (n + 1));
