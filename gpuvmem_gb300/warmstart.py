@@ -346,7 +346,7 @@ def main(argv: Optional[Sequence[str]] = None):
 
         python -m gpuvmem_gb300.warmstart --train 2000 --eval 200 --epochs 80 \
             --shapes 5x16 --pair-iterations 300 \
-            --save gpurun_out/unet_{shape}_p300e80.npz --out gpurun_out/ws_p300e80.json
+            --save unet_{shape}_p300e80.npz --out ws_p300e80.json
 
     (pairs from the plain solver on seeds 1000-2999, each solved for up to
     300 iterations as the evaluation's plain runs are; the held-out skies
