@@ -46,7 +46,6 @@ struct Tile {
   static constexpr int kItems = (sizeof(K) + sizeof(V) > 8) ? 8 : 16;  // per thread
   static constexpr int kChunk = kThreads * kItems;
   static constexpr int kMinBlocks = 2;  // resident per SM
-  static constexpr bool kPrefetch = true;  // next chunk's loads during this one's writes
 };
 constexpr int kSplit = 4;  // counting blocks per tile
 
@@ -176,7 +175,6 @@ __global__ void __launch_bounds__(kThreads, (Tile<K, V>::kMinBlocks)) k_radix_sc
     const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ totals) {
   constexpr int kItems = Tile<K, V>::kItems;
   constexpr int kChunk = Tile<K, V>::kChunk;
-  constexpr bool kPrefetch = Tile<K, V>::kPrefetch;
   __shared__ K sk[kChunk];
   __shared__ V sv[kChunk];
   __shared__ uint32_t cnt[kWarps][kBins];  // per-warp digit counts, then prefixes
@@ -194,10 +192,9 @@ __global__ void __launch_bounds__(kThreads, (Tile<K, V>::kMinBlocks)) k_radix_sc
   // w * 32 * kItems + i * 32 + l, so (w, i, l) is the input order
   K key[kItems];
   V val[kItems];
-  if (kPrefetch) load_chunk<K, V, kItems>(kin, vin, b0, b1, w, lane, key, val);
+  load_chunk<K, V, kItems>(kin, vin, b0, b1, w, lane, key, val);
   for (int64_t base = b0; base < b1; base += kChunk) {
     const int m = (int)dmin(kChunk, b1 - base);
-    if (!kPrefetch) load_chunk<K, V, kItems>(kin, vin, base, b1, w, lane, key, val);
     for (int i = t; i < kWarps * kBins; i += kThreads) (&cnt[0][0])[i] = 0u;
     __syncthreads();
     uint32_t rank[kItems];
@@ -238,7 +235,7 @@ __global__ void __launch_bounds__(kThreads, (Tile<K, V>::kMinBlocks)) k_radix_sc
       }
     }
     // the next chunk's loads go out before this one is written
-    if (kPrefetch) load_chunk<K, V, kItems>(kin, vin, base + kChunk, b1, w, lane, key, val);
+    load_chunk<K, V, kItems>(kin, vin, base + kChunk, b1, w, lane, key, val);
     __syncthreads();
     // sorted position p holds a key of digit d: its place in kout is the
     // digit's running offset plus its rank among the chunk's keys of d

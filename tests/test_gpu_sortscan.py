@@ -103,6 +103,23 @@ def test_sort_u32_bit_ranges(bits):
         assert np.array_equal(v, ev)
 
 
+def test_sort_u32_largest_gridding_slab():
+    """2^27 pairs, the gridding's largest slab, on its 23 cell bits: checked
+    by properties (sorted on the bits, equal keys in input order, a
+    permutation carrying its keys) instead of a host sort of that size"""
+    n = 1 << 27
+    rng = np.random.default_rng(27)
+    keys = rng.integers(0, 1 << 23, n, dtype=np.uint32)
+    keys[rng.random(n) < 0.01] = 0xFFFFFFFF
+    k, v = _sort32(keys, np.arange(n, dtype=np.uint32), 0, 23)
+    sel = k & np.uint32((1 << 23) - 1)
+    assert np.all(sel[1:] >= sel[:-1])
+    same = sel[1:] == sel[:-1]
+    assert np.all(v[1:][same] > v[:-1][same])
+    assert np.all(np.bincount(v, minlength=n) == 1)
+    assert np.array_equal(keys[v], k)
+
+
 @pytest.mark.parametrize("n", [1, 2047, 2048, 2049, 500_003])
 def test_sort_u64(n):
     L = _lib()
