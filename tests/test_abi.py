@@ -67,3 +67,30 @@ def test_null_handles_are_rejected_without_gpu():
     for call in calls:
         assert call() == 1
         assert b"null" in L.gv_last_error()
+
+
+def test_sort_scan_arguments_are_checked_without_gpu():
+    """The device sort / scan / run-length entry points reject null buffers
+    and negative sizes before any CUDA call, and an empty sort or scan is a
+    no-op."""
+    import gpuvmem_gb300 as gv
+    L = gv.lib()
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    sigs = {"gv_radix_sort_pairs_u32": [vp, vp, vp, vp, i64, i32, i32, vp],
+            "gv_radix_sort_pairs_u64": [vp, vp, vp, vp, i64, i32, i32, vp],
+            "gv_exclusive_scan_i32": [vp, vp, i64, vp],
+            "gv_run_length_encode_u32": [vp, i64, vp, vp, vp, i64, vp, vp]}
+    for name, args in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    for fn in (L.gv_radix_sort_pairs_u32, L.gv_radix_sort_pairs_u64):
+        assert fn(None, None, None, None, 0, 0, 32, None) == 0
+        assert fn(None, None, None, None, 16, 0, 32, None) == 1
+        assert b"null" in L.gv_last_error()
+        assert fn(None, None, None, None, -1, 0, 32, None) == 1
+    assert L.gv_exclusive_scan_i32(None, None, 0, None) == 0
+    assert L.gv_exclusive_scan_i32(None, None, 5, None) == 1
+    assert b"null" in L.gv_last_error()
+    assert L.gv_run_length_encode_u32(None, 5, None, None, None, 5, None, None) == 1
+    assert L.gv_run_length_encode_u32(None, -1, None, None, None, 5, None, None) == 1
